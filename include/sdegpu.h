@@ -1,0 +1,196 @@
+/*
+ * sdegpu.h -- C ABI of libsdegpu.so, the GB300 (sm_103a) engine for the
+ * sde-sim-rs path-simulation hot path.
+ *
+ * The drop-in boundary is the reference's whole simulate call: parse the
+ * equation strings once, then advance every scenario through every time
+ * step on the GPU and return the filtration.  The per-step Rust functions
+ * (euler_iteration, runge_kutta_iteration) are far too fine-grained to cross
+ * an FFI or device boundary, so they have no entry point of their own; they
+ * are lowered into the step kernel.
+ *
+ * Conventions
+ *  - Every function returns an int status (SDE_OK = 0); on failure the
+ *    message is kept per thread and read with sde_last_error().  No C++
+ *    exception and no abort crosses the ABI.
+ *  - Plain pointers and sizes only.  "host" buffers are caller-allocated
+ *    host memory; device buffers are cudaMalloc'ed memory of the current
+ *    device; stream arguments are cudaStream_t values (NULL = legacy default
+ *    stream).
+ *  - Objects (sde_plan, sde_result) are engine-owned and released with the
+ *    matching *_destroy call.  A plan may be run from several threads; a
+ *    result belongs to one thread at a time.
+ */
+#ifndef SDEGPU_H
+#define SDEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDE_ABI_VERSION 1
+
+typedef enum sde_status {
+    SDE_OK = 0,
+    SDE_ERR_PARSE = 1,        /* equation/expression grammar (reference: Err(String)) */
+    SDE_ERR_INVALID = 2,      /* bad argument (sizes, unknown scheme, unsorted times) */
+    SDE_ERR_COMPILE = 3,      /* NVRTC lowering failed                                */
+    SDE_ERR_CUDA = 4,         /* CUDA runtime error                                   */
+    SDE_ERR_OOM = 5,          /* device or host allocation failed                     */
+    SDE_ERR_RNG_INDEX = 6,    /* reference panics "RNG Index .. out of bounds"        */
+    SDE_ERR_UNSUPPORTED = 7,  /* combination not built (e.g. > 21201 Sobol dims)      */
+    SDE_ERR_DEVICE = 8        /* a kernel reported a failure through its status word  */
+} sde_status;
+
+enum { SDE_SCHEME_EULER = 0, SDE_SCHEME_RK = 1 };
+enum { SDE_RNG_PSEUDO = 0, SDE_RNG_SOBOL = 1 };
+/* SHIFT: the reference's per-scenario random shift of Sobol point s+5.
+ * XOR:   one random XOR mask per (replicate, dimension), points 0..N-1.      */
+enum { SDE_SCRAMBLE_SHIFT = 0, SDE_SCRAMBLE_XOR = 1 };
+enum { SDE_FP64 = 0, SDE_FP32 = 1 };
+/* REFERENCE: coefficients see the reference's name->value cache exactly as
+ *            src/func.rs:32-42 refreshes it (stale probe state in RK).
+ * TEXTBOOK:  every evaluation sees the state it names.                       */
+enum { SDE_SEM_REFERENCE = 0, SDE_SEM_TEXTBOOK = 1 };
+/* FULL: all time points; CHECKPOINTS: the time indices given at run time;
+ * TERMINAL: the last time point only; NONE: estimators only.                 */
+enum { SDE_OUT_FULL = 0, SDE_OUT_CHECKPOINTS = 1, SDE_OUT_TERMINAL = 2, SDE_OUT_NONE = 3 };
+/* layouts for sde_result_copy_values */
+enum { SDE_LAYOUT_REFERENCE = 0,  /* [replicate][path][time][process]  */
+       SDE_LAYOUT_DEVICE = 1 };   /* [replicate][time][process][path]  */
+
+typedef struct sde_plan sde_plan;
+typedef struct sde_result sde_result;
+
+typedef struct sde_options {
+    uint32_t struct_size;   /* sizeof(sde_options), set by sde_options_init */
+    int32_t scheme;         /* SDE_SCHEME_*        default EULER           */
+    int32_t rng;            /* SDE_RNG_*           default PSEUDO          */
+    int32_t scramble;       /* SDE_SCRAMBLE_*      default SHIFT           */
+    int32_t precision;      /* SDE_FP64 | SDE_FP32 default FP64            */
+    int32_t semantics;      /* SDE_SEM_*           default REFERENCE       */
+    int32_t output;         /* SDE_OUT_*           default FULL            */
+    int32_t block_size;     /* threads per block, 0 = 256                  */
+    int32_t reserved[8];
+} sde_options;
+
+typedef struct sde_run_args {
+    uint32_t struct_size;       /* sizeof(sde_run_args), set by sde_run_args_init */
+    const double* times;        /* host [n_times], strictly increasing            */
+    int32_t n_times;
+    const double* x0;           /* host [n_x0] time-0 row by process index;
+                                   missing processes start at 0.0              */
+    int32_t n_x0;
+    const double* params;       /* host [n_params] values of the named params   */
+    int32_t n_params;
+    uint64_t n_paths;           /* paths per replicate                          */
+    int32_t n_replicates;       /* >= 1                                         */
+    uint64_t seed;              /* scenario s uses ChaCha8 seed_from_u64(seed+s);
+                                   XOR replicate r uses masks from seed + r     */
+    uint64_t path_offset;       /* scenario index of path 0 (default 0)         */
+    const int32_t* checkpoints; /* host time indices for SDE_OUT_CHECKPOINTS    */
+    int32_t n_checkpoints;
+    void* stream;               /* cudaStream_t or NULL                         */
+    void* device_out;           /* optional caller-owned device buffer for the
+                                   filtration (device layout); NULL = engine    */
+    uint64_t device_out_bytes;
+} sde_run_args;
+
+/* ---- version / errors ------------------------------------------------- */
+int32_t sde_abi_version(void);
+/* Copies the calling thread's last error message (NUL-terminated). */
+int sde_last_error(char* buf, size_t buf_len);
+
+void sde_options_init(sde_options* opts);
+void sde_run_args_init(sde_run_args* args);
+
+/* ---- plans -------------------------------------------------------------
+ * Replaces sde_sim_rs::proc::util::parse_equations
+ *   (src/proc/util.rs:52-55, -> ProcessUniverse src/proc/mod.rs:70-89)
+ * and the per-call fasteval compilation of every coefficient
+ *   (src/func.rs:18-30): the universe is lowered to one sm_103a kernel with
+ * NVRTC.  param_names declares names that expressions may use besides the
+ * processes and t (values are given per run).  payoffs are estimator
+ * expressions over the terminal state (empty for none).                   */
+int sde_plan_create(const char* const* equations, int32_t n_equations,
+                    const char* const* param_names, int32_t n_params,
+                    const char* const* payoffs, int32_t n_payoffs,
+                    const sde_options* opts, sde_plan** out_plan);
+int sde_plan_destroy(sde_plan* plan);
+int sde_plan_n_processes(const sde_plan* plan, int32_t* n);
+int sde_plan_n_stochastic(const sde_plan* plan, int32_t* n);
+/* ProcessUniverse.processes[i].name() (src/proc/mod.rs:46-59) */
+int sde_plan_process_name(const sde_plan* plan, int32_t i, char* buf, size_t buf_len);
+/* ProcessUniverse.process_registry lookup; *index = -1 if absent */
+int sde_plan_process_index(const sde_plan* plan, const char* name, int32_t* index);
+/* ProcessUniverse.stochastic_registry, index -> token (src/proc/util.rs:145-146) */
+int sde_plan_stochastic_token(const sde_plan* plan, int32_t i, char* buf, size_t buf_len);
+/* The generated CUDA C (for inspection); *needed gets the size incl. NUL. */
+int sde_plan_source(const sde_plan* plan, char* buf, size_t buf_len, size_t* needed);
+
+/* ---- runs --------------------------------------------------------------
+ * Replaces the scenario loop of sde_sim_rs::sim::simulate
+ *   (src/sim/mod.rs:41-88: per-scenario filtration, RNG, step loop).
+ * Asynchronous on args->stream; results are read through sde_result_*.   */
+int sde_run(sde_plan* plan, const sde_run_args* args, sde_result** out_result);
+
+/* Reference-shaped one-shot entry: sde_sim_rs::sim::simulate
+ *   (src/sim/mod.rs:20-27) and simulate_py (src/py_binding.rs:10-18).
+ * scheme "euler" | "runge-kutta" (else SDE_ERR_INVALID; the reference
+ * panics); rng_method "sobol" or anything else = pseudo (src/sim/mod.rs:65).
+ * FP64, reference semantics, full filtration.  has_seed = 0 draws the seed
+ * from the OS like src/sim/mod.rs:28-29.                                   */
+int sde_simulate(const char* const* equations, int32_t n_equations,
+                 const double* times, int32_t n_times,
+                 const char* const* init_names, const double* init_values, int32_t n_init,
+                 uint64_t n_scenarios, const char* scheme, const char* rng_method,
+                 uint64_t seed, int32_t has_seed, sde_result** out_result);
+
+/* ---- results ------------------------------------------------------------ */
+int sde_result_destroy(sde_result* r);
+/* Blocks until the run finished; reports a device status failure. */
+int sde_result_wait(sde_result* r);
+int sde_result_shape(const sde_result* r, uint64_t* n_paths, int32_t* n_out_times,
+                     int32_t* n_processes, int32_t* n_replicates);
+/* Time indices of the output slots [n_out_times]. */
+int sde_result_time_indices(const sde_result* r, int32_t* host_out);
+/* Device pointer of the filtration, layout [rep][time][process][path]. */
+int sde_result_device_values(const sde_result* r, void** device_ptr, int32_t* elem_bytes);
+/* Filtration copied to host as f64 in the given SDE_LAYOUT_*. */
+int sde_result_copy_values(sde_result* r, double* host_out, int32_t layout);
+/* Long / tidy rows in the reference's order (scenario, time, process),
+ * the columns of ScenarioFiltration::to_lazyframe + concat
+ *   (src/filtration.rs:81-116, src/sim/mod.rs:91).  Each host array has
+ * n_replicates * n_paths * n_out_times * n_processes entries; any may be
+ * NULL.  Built on the device, then copied.                                 */
+int sde_result_copy_long(sde_result* r, int32_t* scenario, double* time,
+                         int32_t* process, double* value);
+/* Per replicate and estimator: sum and sum of squares of the payoff over
+ * paths, FP64 with compensated summation; arrays [n_replicates][n_payoffs]. */
+int sde_result_estimates(sde_result* r, double* host_sum, double* host_sumsq);
+
+/* ---- known-answer kernels (device versions of the RNG building blocks) --
+ * rand_chacha ChaCha8Rng::seed_from_u64(seed), u64 values [first, first+n)
+ *   (src/rng/pseudo.rs:14-31).                                             */
+int sde_kat_chacha8_u64(uint64_t seed, uint64_t first, uint64_t n, uint64_t* host_out);
+/* Joe-Kuo D6 Sobol points [first, first+n) x dims as uint32
+ *   (sobol crate via src/rng/sobol.rs:15-25).                              */
+int sde_kat_sobol_points(int32_t dims, uint64_t first, uint64_t n, uint32_t* host_out);
+/* fast_inverse_normal_cdf over host p[n] in FP64 (src/proc/increment.rs:161-179). */
+int sde_kat_icdf(const double* host_p, uint64_t n, double* host_out);
+/* Host-side Joe-Kuo direction numbers [dims][32] (no GPU needed). */
+int sde_sobol_directions(int32_t dims, uint32_t* host_out);
+
+/* ---- measurement helper ------------------------------------------------
+ * Times a kernel that keeps the SFU (MUFU) pipe busy and reports its
+ * throughput in operations per second; the roofline denominator of the
+ * terminal-only (SFU-bound) kernels.                                       */
+int sde_probe_sfu_peak(double* ops_per_second);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,43 @@
+// codegen.h -- lowering of a parsed process universe to sm_103a device code.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "frontend.h"
+
+namespace sde {
+
+enum Scheme { SCHEME_EULER = 0, SCHEME_RK = 1 };
+enum RngKind { RNG_PSEUDO = 0, RNG_SOBOL = 1 };
+enum Scramble { SCRAMBLE_SHIFT = 0, SCRAMBLE_XOR = 1 };
+enum Precision { PREC_FP64 = 0, PREC_FP32 = 1 };
+enum Semantics { SEM_REFERENCE = 0, SEM_TEXTBOOK = 1 };
+
+struct KernelSpec {
+    int scheme = SCHEME_EULER;
+    int rng = RNG_PSEUDO;
+    int scramble = SCRAMBLE_SHIFT;
+    int precision = PREC_FP64;
+    int semantics = SEM_REFERENCE;
+    bool store_output = true;           // filtration slices selected by out_tidx
+    std::vector<ExprP> payoffs;         // resolved estimator expressions
+    int block = 256;
+    // adjoint: parameters and initial values to differentiate
+    bool adjoint = false;
+    std::vector<int> grad_params;       // parameter indices
+    std::vector<int> grad_x0;           // process indices
+};
+
+// Name of the forward kernel in the generated source.
+std::string forward_kernel_name(const KernelSpec& s);
+std::string adjoint_kernel_name(const KernelSpec& s);
+
+// CUDA C source of the kernels for one universe (without the runtime
+// header, which the JIT prepends).
+std::string generate_source(const Universe& u, const KernelSpec& s);
+
+// Expression emitter, exposed for tests of the lowering.
+std::string emit_expression(const ExprP& e, bool fp32);
+
+}  // namespace sde

@@ -1,0 +1,252 @@
+/*
+ * sde_rt.cuh -- device runtime of the GB300 path-simulation engine.
+ *
+ * Included by the nvcc-built kernels (kernels.cu) and prepended to every
+ * NVRTC-lowered step kernel.  It holds the per-path random streams, the
+ * Sobol point construction, the inverse CDFs, the fasteval operator
+ * semantics and the estimator reduction.  No system headers: NVRTC builds
+ * it without an include path.
+ */
+#ifndef SDE_RT_CUH
+#define SDE_RT_CUH
+
+#define SDE_DEV static __device__ __forceinline__
+#define SDE_FULL_MASK 0xffffffffu
+
+/* ------------------------------------------------------------------------
+ * ChaCha8 per scenario (rand_chacha 0.9 as called at src/rng/pseudo.rs:18
+ * and src/rng/sobol.rs:68): 32-byte key from rand_core's PCG32-based
+ * seed_from_u64, 64-bit block counter in words 12-13 starting at 0,
+ * stream 0 in words 14-15, 8 rounds.  u64 number k of the stream is words
+ * 2k (low) and 2k+1 (high).
+ * ---------------------------------------------------------------------- */
+
+SDE_DEV sde_u32 sde_rotl(sde_u32 x, int n) { return __funnelshift_l(x, x, n); }
+
+SDE_DEV void sde_seed_from_u64(sde_u64 s, sde_u32 k[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        s = s * 6364136223846793005ull + 11634580027462260723ull;
+        const sde_u32 xs = (sde_u32)(((s >> 18) ^ s) >> 27);
+        const sde_u32 rot = (sde_u32)(s >> 59);
+        k[i] = __funnelshift_r(xs, xs, rot);
+    }
+}
+
+#define SDE_QR(a, b, c, d)                          \
+    a += b; d ^= a; d = sde_rotl(d, 16);            \
+    c += d; b ^= c; b = sde_rotl(b, 12);            \
+    a += b; d ^= a; d = sde_rotl(d, 8);             \
+    c += d; b ^= c; b = sde_rotl(b, 7);
+
+SDE_DEV void sde_chacha8_block(const sde_u32 k[8], sde_u64 ctr, sde_u32 o[16]) {
+    sde_u32 x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
+    sde_u32 x4 = k[0], x5 = k[1], x6 = k[2], x7 = k[3];
+    sde_u32 x8 = k[4], x9 = k[5], x10 = k[6], x11 = k[7];
+    const sde_u32 c0 = (sde_u32)ctr, c1 = (sde_u32)(ctr >> 32);
+    sde_u32 x12 = c0, x13 = c1, x14 = 0u, x15 = 0u;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        SDE_QR(x0, x4, x8, x12) SDE_QR(x1, x5, x9, x13)
+        SDE_QR(x2, x6, x10, x14) SDE_QR(x3, x7, x11, x15)
+        SDE_QR(x0, x5, x10, x15) SDE_QR(x1, x6, x11, x12)
+        SDE_QR(x2, x7, x8, x13) SDE_QR(x3, x4, x9, x14)
+    }
+    o[0] = x0 + 0x61707865u; o[1] = x1 + 0x3320646eu;
+    o[2] = x2 + 0x79622d32u; o[3] = x3 + 0x6b206574u;
+    o[4] = x4 + k[0]; o[5] = x5 + k[1]; o[6] = x6 + k[2]; o[7] = x7 + k[3];
+    o[8] = x8 + k[4]; o[9] = x9 + k[5]; o[10] = x10 + k[6]; o[11] = x11 + k[7];
+    o[12] = x12 + c0; o[13] = x13 + c1; o[14] = x14; o[15] = x15;
+}
+
+SDE_DEV sde_u64 sde_pair(sde_u32 lo, sde_u32 hi) { return ((sde_u64)hi << 32) | (sde_u64)lo; }
+
+/* rand's StandardUniform<f64>: (u64 >> 11) * 2^-53 */
+SDE_DEV double sde_u64_to_f64(sde_u64 r) { return (double)(r >> 11) * 0x1p-53; }
+
+/* ------------------------------------------------------------------------
+ * Uniform tail probabilities for the FP32 kernels: q = min(p, 1-p) formed
+ * exactly in integers, so the only rounding is the final float conversion.
+ * up is p >= 0.5, gt is p > 0.5.
+ * ---------------------------------------------------------------------- */
+
+/* pseudo: p = U * 2^-53, U = r >> 11 */
+SDE_DEV void sde_tail_u53(sde_u64 U, float& q, bool& up, bool& gt) {
+    up = U >= (1ull << 52);
+    gt = U > (1ull << 52);
+    const sde_u64 Q = up ? (1ull << 53) - U : U;
+    q = __ull2float_rn(Q) * 0x1p-53f;
+}
+
+/* Sobol with a random shift (src/rng/sobol.rs:62-79): u = fract(x*2^-32 + s)
+ * in f64, s = (r >> 11)*2^-53.  Emulated exactly in 53-bit fixed point:
+ * sums in [1,2) round to a multiple of 2^-52, ties to even. */
+SDE_DEV sde_u64 sde_shift_u53(sde_u32 x, sde_u64 r) {
+    const sde_u64 sum = ((sde_u64)x << 21) + (r >> 11);
+    if (sum < (1ull << 53)) return sum;
+    sde_u64 h = sum >> 1;
+    if ((sum & 1ull) && (h & 1ull)) h += 1ull;
+    return (h - (1ull << 52)) << 1;
+}
+
+/* XOR-scrambled Sobol: p = (y + 0.5) * 2^-32 */
+SDE_DEV void sde_tail_xor(sde_u32 y, float& q, bool& up, bool& gt) {
+    up = (y >> 31) != 0u;
+    gt = up;
+    const sde_u32 m = up ? ~y : y;
+    q = __uint2float_rn(2u * m + 1u) * 0x1p-33f;
+}
+
+/* ------------------------------------------------------------------------
+ * Sobol points (sobol crate, Joe-Kuo D6, Gray-code order):
+ *   x_n[d] = xor of V[d][b] over the set bits b of gray(n) = n ^ (n >> 1).
+ * ---------------------------------------------------------------------- */
+
+SDE_DEV sde_u32 sde_gray(sde_u32 n) { return n ^ (n >> 1); }
+
+SDE_DEV sde_u32 sde_sobol_direct(const sde_u32* __restrict__ V, int d, sde_u32 g) {
+    const sde_u32* v = V + (sde_u64)d * 32u;
+    sde_u32 x = 0u;
+    while (g) {
+        const int b = __ffs(g) - 1;
+        x ^= __ldg(v + b);
+        g &= g - 1u;
+    }
+    return x;
+}
+
+/* Warp-cooperative part of a point: for a warp whose 32 lanes hold points
+ * 32w .. 32w+31, gray(n) >> 5 == gray(w) is the same on every lane.  Lane l
+ * returns, for dimension 32*chunk + l, the xor of the direction numbers
+ * 5.. selected by H = gray(w), xored with the scramble mask; lanes then
+ * fetch a dimension's value with one shuffle. */
+SDE_DEV sde_u32 sde_sobol_hi(const sde_u32* __restrict__ VT, const sde_u32* __restrict__ mask,
+                             int dims, int chunk, sde_u32 H, int lane) {
+    const int d = chunk * 32 + lane;
+    if (d >= dims) return 0u;
+    /* mask rows are padded to a multiple of 32 words */
+    sde_u32 acc = mask ? __ldg(mask + d) : 0u;
+    while (H) {
+        const int b = __ffs(H) - 1;
+        acc ^= __ldg(VT + (sde_u64)(b + 5) * (sde_u64)dims + (sde_u64)d);
+        H &= H - 1u;
+    }
+    return acc;
+}
+
+/* ------------------------------------------------------------------------
+ * Inverse CDFs (src/proc/increment.rs:161-200)
+ * ---------------------------------------------------------------------- */
+
+/* Abramowitz-Stegun 26.2.23, exactly as the reference evaluates it. */
+SDE_DEV double sde_icdf_as26(double p) {
+    const double t = p < 0.5 ? sqrt(-2.0 * log(p)) : sqrt(-2.0 * log(1.0 - p));
+    const double x = t - ((0.010328 * t + 0.802853) * t + 2.515517) /
+                             (((0.001308 * t + 0.189269) * t + 1.432788) * t + 1.0);
+    return p < 0.5 ? -x : x;
+}
+
+/* The same rational approximation in FP32, from the exact tail q. */
+SDE_DEV float sde_icdf_as26_q(float q, bool up) {
+    const float t = sqrtf(-2.0f * __logf(q));
+    const float num = (0.010328f * t + 0.802853f) * t + 2.515517f;
+    const float den = ((0.001308f * t + 0.189269f) * t + 1.432788f) * t + 1.0f;
+    const float x = t - __fdividef(num, den);
+    return up ? x : -x;
+}
+
+/* Poisson inverse CDF with the reference's cap of 200 (increment.rs:182-200) */
+SDE_DEV double sde_poisson(double u, double lambda) {
+    if (lambda <= 0.0) return 0.0;
+    double p = exp(-lambda);
+    double f = p;
+    int k = 0;
+    while (u > f && k < 200) {
+        k += 1;
+        p *= lambda / (double)k;
+        f += p;
+    }
+    return (double)k;
+}
+
+SDE_DEV float sde_poisson(float u, float lambda) {
+    if (lambda <= 0.0f) return 0.0f;
+    float p = expf(-lambda);
+    float f = p;
+    int k = 0;
+    while (u > f && k < 200) {
+        k += 1;
+        p *= lambda / (float)k;
+        f += p;
+    }
+    return (float)k;
+}
+
+/* ------------------------------------------------------------------------
+ * fasteval operator semantics (src/func.rs:18-42 evaluates with fasteval
+ * 0.2.4): comparisons give 1/0, == != <= >= carry fasteval's 8*eps absolute
+ * tolerance, && and || return an operand, log(x) is ln(x)/ln(10).
+ * ---------------------------------------------------------------------- */
+
+#define SDE_EPS8 0x1p-49
+
+SDE_DEV double sde_b(bool b, double) { return b ? 1.0 : 0.0; }
+SDE_DEV float sde_b(bool b, float) { return b ? 1.0f : 0.0f; }
+template <class R> SDE_DEV R sde_eq(R l, R r) { return sde_b(fabs(l - r) <= (R)SDE_EPS8, l); }
+template <class R> SDE_DEV R sde_ne(R l, R r) { return sde_b(fabs(l - r) > (R)SDE_EPS8, l); }
+template <class R> SDE_DEV R sde_lt(R l, R r) { return sde_b(l < r, l); }
+template <class R> SDE_DEV R sde_gt(R l, R r) { return sde_b(l > r, l); }
+template <class R> SDE_DEV R sde_le(R l, R r) { return sde_b(l <= r + (R)SDE_EPS8, l); }
+template <class R> SDE_DEV R sde_ge(R l, R r) { return sde_b(l + (R)SDE_EPS8 >= r, l); }
+template <class R> SDE_DEV R sde_not(R x) { return sde_b(fabs(x) <= (R)SDE_EPS8, x); }
+template <class R> SDE_DEV R sde_and(R l, R r) { return fabs(l) <= (R)SDE_EPS8 ? l : r; }
+template <class R> SDE_DEV R sde_or(R l, R r) { return fabs(l) > (R)SDE_EPS8 ? l : r; }
+template <class R> SDE_DEV R sde_sign(R x) { return isnan(x) ? x : (signbit(x) ? (R)-1 : (R)1); }
+template <class R> SDE_DEV R sde_sq(R x) { return x * x; }
+SDE_DEV double sde_log10(double x) { return log(x) / 0x1.26bb1bbb55516p+1; }
+SDE_DEV float sde_log10(float x) { return logf(x) / 0x1.26bb1cp+1f; }
+template <class R> SDE_DEV R sde_logb(R b, R x) { return log(x) / log(b); }
+template <class R> SDE_DEV R sde_round2(R m, R x) { return round(x / m) * m; }
+
+/* ------------------------------------------------------------------------
+ * Estimator reduction (fused epilogue): warp shuffles, then a Neumaier
+ * compensated sum over the block's warps, in FP64.  out gets
+ * {sum, compensation, sum of squares, compensation} per estimator.
+ * ---------------------------------------------------------------------- */
+
+SDE_DEV void sde_neumaier(double& s, double& c, double x) {
+    const double t = s + x;
+    if (fabs(s) >= fabs(x)) c += (s - t) + x;
+    else c += (x - t) + s;
+    s = t;
+}
+
+template <int K>
+SDE_DEV void sde_block_reduce_store(const double (&f)[K], double* __restrict__ out) {
+    __shared__ double sm[K][32][2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = f[k], q = f[k] * f[k];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            s += __shfl_down_sync(SDE_FULL_MASK, s, o);
+            q += __shfl_down_sync(SDE_FULL_MASK, q, o);
+        }
+        if (lane == 0) { sm[k][warp][0] = s; sm[k][warp][1] = q; }
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        const int k = threadIdx.x;
+        double s = 0.0, sc = 0.0, q = 0.0, qc = 0.0;
+        for (int w = 0; w < nw; ++w) {
+            sde_neumaier(s, sc, sm[k][w][0]);
+            sde_neumaier(q, qc, sm[k][w][1]);
+        }
+        out[k * 4 + 0] = s; out[k * 4 + 1] = sc;
+        out[k * 4 + 2] = q; out[k * 4 + 3] = qc;
+    }
+}
+
+#endif

@@ -1,0 +1,891 @@
+// engine.cpp -- plans, runs and results behind the C ABI (include/sdegpu.h).
+//
+// A plan is the reference's parse_equations (src/proc/util.rs:52-66) plus a
+// one-time lowering of every coefficient to device code: the generated CUDA
+// C is compiled by NVRTC for sm_103a and loaded per device with
+// cudaLibraryLoadData.  A run replaces the scenario loop of sim::simulate
+// (src/sim/mod.rs:41-88) with one kernel launch over (paths x replicates).
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <random>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/sdegpu.h"
+#include "_gen/embedded.h"
+#include "_gen/joe_kuo_d6.h"
+#include "codegen.h"
+#include "frontend.h"
+#include "kernels.h"
+
+namespace sde {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+
+static thread_local std::string g_last_error;
+
+struct Error {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] static void fail(int code, const std::string& msg) { throw Error{code, msg}; }
+
+static void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        if (e == cudaErrorMemoryAllocation) fail(SDE_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+        fail(SDE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+template <class F>
+static int guarded(F&& f) {
+    try {
+        f();
+        return SDE_OK;
+    } catch (const Error& e) {
+        g_last_error = e.msg;
+        return e.code;
+    } catch (const ParseError& e) {
+        g_last_error = e.what();
+        return SDE_ERR_PARSE;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return SDE_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return SDE_ERR_INVALID;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// memory pools: device buffers and pinned host buffers are cached by size so
+// repeated runs do not pay cudaMalloc / cudaHostAlloc.
+// ---------------------------------------------------------------------------
+
+static size_t round_size(size_t n) {
+    if (n <= 256) return 256;
+    if (n <= (1u << 20)) {
+        size_t r = 256;
+        while (r < n) r <<= 1;
+        return r;
+    }
+    const size_t g = 1u << 20;
+    return (n + g - 1) / g * g;
+}
+
+struct Pool {
+    bool pinned;
+    std::mutex mu;
+    std::map<std::pair<int, size_t>, std::vector<void*>> free_;
+    std::unordered_map<void*, std::pair<int, size_t>> live_;
+
+    explicit Pool(bool p) : pinned(p) {}
+
+    void* get(size_t n) {
+        int dev = 0;
+        if (!pinned) cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+        const size_t sz = round_size(n);
+        {
+            std::lock_guard<std::mutex> g(mu);
+            auto it = free_.find({dev, sz});
+            if (it != free_.end() && !it->second.empty()) {
+                void* p = it->second.back();
+                it->second.pop_back();
+                live_[p] = {dev, sz};
+                return p;
+            }
+        }
+        void* p = nullptr;
+        cudaError_t e = pinned ? cudaHostAlloc(&p, sz, cudaHostAllocDefault) : cudaMalloc(&p, sz);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            trim(dev);
+            e = pinned ? cudaHostAlloc(&p, sz, cudaHostAllocDefault) : cudaMalloc(&p, sz);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                fail(SDE_ERR_OOM, std::string(pinned ? "cudaHostAlloc" : "cudaMalloc") + " of " +
+                                      std::to_string(sz) + " bytes failed");
+            }
+        }
+        std::lock_guard<std::mutex> g(mu);
+        live_[p] = {dev, sz};
+        return p;
+    }
+    void put(void* p) {
+        if (!p) return;
+        std::lock_guard<std::mutex> g(mu);
+        auto it = live_.find(p);
+        if (it == live_.end()) return;
+        free_[it->second].push_back(p);
+        live_.erase(it);
+    }
+    void trim(int dev) {
+        std::lock_guard<std::mutex> g(mu);
+        for (auto& kv : free_) {
+            if (!pinned && kv.first.first != dev) continue;
+            for (void* p : kv.second) pinned ? cudaFreeHost(p) : cudaFree(p);
+            kv.second.clear();
+        }
+    }
+};
+
+static Pool& dpool() { static Pool* p = new Pool(false); return *p; }
+static Pool& hpool() { static Pool* p = new Pool(true); return *p; }
+
+struct DBuf {
+    void* p = nullptr;
+    DBuf() = default;
+    explicit DBuf(size_t n) : p(n ? dpool().get(n) : nullptr) {}
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p) { o.p = nullptr; }
+    DBuf& operator=(DBuf&& o) noexcept { std::swap(p, o.p); return *this; }
+    ~DBuf() { dpool().put(p); }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+struct HBuf {
+    void* p = nullptr;
+    HBuf() = default;
+    explicit HBuf(size_t n) : p(n ? hpool().get(n) : nullptr) {}
+    HBuf(const HBuf&) = delete;
+    HBuf& operator=(const HBuf&) = delete;
+    HBuf(HBuf&& o) noexcept : p(o.p) { o.p = nullptr; }
+    HBuf& operator=(HBuf&& o) noexcept { std::swap(p, o.p); return *this; }
+    ~HBuf() { hpool().put(p); }
+    template <class T> T* as() const { return (T*)p; }
+};
+
+// ---------------------------------------------------------------------------
+// Joe-Kuo D6 direction numbers.  Scaled form of the Bratley-Fox recurrence:
+//   v_k = v_{k-s} ^ (v_{k-s} >> s) ^ xor_{i<s} a_i v_{k-i},  v_k = m_k 2^(32-k)
+// ---------------------------------------------------------------------------
+
+static const int kSobolMaxDims = kJkDims;
+
+static void sobol_directions_host(int dims, uint32_t* V) {
+    for (int d = 0; d < dims; ++d) {
+        uint32_t* v = V + (size_t)d * 32;
+        if (d == 0) {
+            for (int k = 0; k < 32; ++k) v[k] = 0x80000000u >> k;
+            continue;
+        }
+        const uint32_t poly = kJkPoly[d];
+        int s = 31;
+        while (!((poly >> s) & 1u)) --s;
+        for (int k = 0; k < s && k < 32; ++k) v[k] = kJkVinit[(size_t)d * 18 + k] << (31 - k);
+        for (int k = s; k < 32; ++k) {
+            uint32_t x = v[k - s] ^ (v[k - s] >> s);
+            for (int i = 1; i < s; ++i)
+                if ((poly >> (s - i)) & 1u) x ^= v[k - i];
+            v[k] = x;
+        }
+    }
+}
+
+struct SobolTables {
+    DBuf V, VT, LO;
+    int dims = 0;
+};
+
+static std::mutex g_tab_mu;
+static std::map<int, std::unique_ptr<SobolTables>> g_tables;  // by device
+
+static SobolTables& sobol_tables(cudaStream_t stream) {
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> g(g_tab_mu);
+    auto& t = g_tables[dev];
+    if (t) return *t;
+    const int dims = kSobolMaxDims;
+    std::vector<uint32_t> V((size_t)dims * 32), VT((size_t)dims * 32), LO((size_t)dims * 32);
+    sobol_directions_host(dims, V.data());
+    for (int d = 0; d < dims; ++d)
+        for (int b = 0; b < 32; ++b) VT[(size_t)b * dims + d] = V[(size_t)d * 32 + b];
+    for (int d = 0; d < dims; ++d)
+        for (int l = 0; l < 32; ++l) {
+            uint32_t x = 0;
+            for (int b = 0; b < 5; ++b)
+                if ((l >> b) & 1) x ^= V[(size_t)d * 32 + b];
+            LO[(size_t)d * 32 + l] = x;
+        }
+    auto nt = std::make_unique<SobolTables>();
+    const size_t bytes = (size_t)dims * 32 * 4;
+    nt->V = DBuf(bytes);
+    nt->VT = DBuf(bytes);
+    nt->LO = DBuf(bytes);
+    cuda_check(cudaMemcpyAsync(nt->V.p, V.data(), bytes, cudaMemcpyHostToDevice, stream), "upload Sobol V");
+    cuda_check(cudaMemcpyAsync(nt->VT.p, VT.data(), bytes, cudaMemcpyHostToDevice, stream), "upload Sobol VT");
+    cuda_check(cudaMemcpyAsync(nt->LO.p, LO.data(), bytes, cudaMemcpyHostToDevice, stream), "upload Sobol LO");
+    cuda_check(cudaStreamSynchronize(stream), "Sobol tables");
+    nt->dims = dims;
+    t = std::move(nt);
+    return *t;
+}
+
+// ---------------------------------------------------------------------------
+// JIT: NVRTC -> cubin (cached by source), cudaLibrary per device
+// ---------------------------------------------------------------------------
+
+struct Cubin {
+    std::vector<char> image;
+    std::string log;
+};
+
+static std::mutex g_jit_mu;
+static std::unordered_map<std::string, std::shared_ptr<Cubin>> g_cubins;
+
+static std::shared_ptr<Cubin> compile_cubin(const std::string& gen_src, bool fp32) {
+    std::string src = std::string(kEmbArgs) + "\n" + kEmbRt + "\n" + gen_src;
+    const std::string key = std::string(fp32 ? "f32|" : "f64|") + src;
+    {
+        std::lock_guard<std::mutex> g(g_jit_mu);
+        auto it = g_cubins.find(key);
+        if (it != g_cubins.end()) return it->second;
+    }
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "sde_plan.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        fail(SDE_ERR_COMPILE, "nvrtcCreateProgram failed");
+    std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device"};
+    if (fp32) {
+        opts.push_back("-ftz=true");
+        opts.push_back("-prec-div=false");
+        opts.push_back("-prec-sqrt=false");
+        opts.push_back("-fmad=true");
+    } else {
+        // the reference never contracts a*b+c; keep every product rounded
+        opts.push_back("-fmad=false");
+    }
+    nvrtcResult r = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
+    auto c = std::make_shared<Cubin>();
+    size_t ls = 0;
+    nvrtcGetProgramLogSize(prog, &ls);
+    c->log.resize(ls);
+    if (ls) nvrtcGetProgramLog(prog, &c->log[0]);
+    if (r != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        fail(SDE_ERR_COMPILE, std::string("NVRTC: ") + nvrtcGetErrorString(r) + "\n" + c->log);
+    }
+    size_t cs = 0;
+    nvrtcGetCUBINSize(prog, &cs);
+    c->image.resize(cs);
+    nvrtcGetCUBIN(prog, c->image.data());
+    nvrtcDestroyProgram(&prog);
+    std::lock_guard<std::mutex> g(g_jit_mu);
+    g_cubins[key] = c;
+    return c;
+}
+
+struct Loaded {
+    cudaLibrary_t lib = nullptr;
+    cudaKernel_t fwd = nullptr;
+    cudaKernel_t adj = nullptr;
+};
+
+// ---------------------------------------------------------------------------
+// plans and results
+// ---------------------------------------------------------------------------
+
+}  // namespace sde
+
+struct sde_plan {
+    sde::Universe u;
+    sde::KernelSpec spec;
+    int output = SDE_OUT_FULL;
+    std::string source;
+    std::string fwd_name;
+    std::shared_ptr<sde::Cubin> cubin;
+    std::mutex mu;
+    std::map<int, sde::Loaded> loaded;  // by device
+};
+
+struct sde_result {
+    std::shared_ptr<sde_plan> plan_keep;  // keeps the plan alive for one-shot runs
+    sde_plan* plan = nullptr;
+    uint64_t n_paths = 0;
+    int n_rep = 1, n_out = 0, P = 0, K = 0, elem = 8;
+    uint64_t scen_base = 0;
+    std::vector<int32_t> slot_tidx;
+    std::vector<double> slot_times;
+    sde::DBuf out;                 // engine-owned filtration
+    void* out_ptr = nullptr;       // filtration (engine- or caller-owned)
+    sde::DBuf args_dev;            // staged time grid etc.
+    sde::DBuf partials, est_dev, masks;
+    sde::HBuf est_host;
+    sde::HBuf stage;               // pinned inputs, alive until the run is done
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    int* status_dev = nullptr;
+    sde::HBuf status_host;
+    bool waited = false;
+};
+
+namespace sde {
+
+static Loaded& ensure_loaded(sde_plan* p) {
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> g(p->mu);
+    Loaded& L = p->loaded[dev];
+    if (!L.lib) {
+        cuda_check(cudaLibraryLoadData(&L.lib, p->cubin->image.data(), nullptr, nullptr, 0, nullptr,
+                                       nullptr, 0),
+                   "cudaLibraryLoadData");
+        cuda_check(cudaLibraryGetKernel(&L.fwd, L.lib, p->fwd_name.c_str()), "cudaLibraryGetKernel");
+    }
+    return L;
+}
+
+static KernelSpec spec_from(const sde_options* o) {
+    KernelSpec s;
+    s.scheme = o->scheme;
+    s.rng = o->rng;
+    s.scramble = o->scramble;
+    s.precision = o->precision;
+    s.semantics = o->semantics;
+    s.store_output = o->output != SDE_OUT_NONE;
+    s.block = o->block_size > 0 ? o->block_size : 256;
+    if (s.scheme != SCHEME_EULER && s.scheme != SCHEME_RK) fail(SDE_ERR_INVALID, "unknown scheme");
+    if (s.rng != RNG_PSEUDO && s.rng != RNG_SOBOL) fail(SDE_ERR_INVALID, "unknown rng");
+    if (s.scramble != SCRAMBLE_SHIFT && s.scramble != SCRAMBLE_XOR) fail(SDE_ERR_INVALID, "unknown scramble");
+    if (s.precision != PREC_FP64 && s.precision != PREC_FP32) fail(SDE_ERR_INVALID, "unknown precision");
+    if (s.semantics != SEM_REFERENCE && s.semantics != SEM_TEXTBOOK) fail(SDE_ERR_INVALID, "unknown semantics");
+    if (o->output < SDE_OUT_FULL || o->output > SDE_OUT_NONE) fail(SDE_ERR_INVALID, "unknown output mode");
+    if (s.block % 32 != 0 || s.block > 1024) fail(SDE_ERR_INVALID, "block_size must be a multiple of 32 up to 1024");
+    return s;
+}
+
+static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vector<std::string>& params,
+                             const std::vector<std::string>& payoffs, const sde_options& o) {
+    auto p = std::make_unique<sde_plan>();
+    p->u = parse_universe(eqs, params);
+    p->spec = spec_from(&o);
+    p->output = o.output;
+    for (const auto& s : payoffs) p->spec.payoffs.push_back(p->u.resolve(parse_expression(s)));
+    if ((int)p->spec.payoffs.size() > 32) fail(SDE_ERR_INVALID, "at most 32 payoffs");
+    p->fwd_name = forward_kernel_name(p->spec);
+    p->source = generate_source(p->u, p->spec);
+    p->cubin = compile_cubin(p->source, p->spec.precision == PREC_FP32);
+    return p.release();
+}
+
+static sde_result* run(sde_plan* p, const sde_run_args& a) {
+    const Universe& u = p->u;
+    const int P = u.n_processes(), NI = u.n_stochastic(), T = a.n_times;
+    if (T < 1 || !a.times) fail(SDE_ERR_INVALID, "need at least one time point");
+    for (int t = 1; t < T; ++t)
+        if (!(a.times[t] > a.times[t - 1])) fail(SDE_ERR_INVALID, "time_steps must be strictly increasing");
+    if (a.n_replicates < 1) fail(SDE_ERR_INVALID, "n_replicates must be >= 1");
+    if (a.n_replicates > 65535) fail(SDE_ERR_INVALID, "at most 65535 replicates");
+    if (a.n_params != (int)u.params.size()) fail(SDE_ERR_INVALID, "parameter count does not match the plan");
+    if (a.n_x0 > P) fail(SDE_ERR_INVALID, "more initial values than processes");
+    if (p->spec.scheme == SCHEME_RK && NI == 0 && T > 1)
+        fail(SDE_ERR_RNG_INDEX, "RNG Index 0 out of bounds (max 0)");
+    const uint64_t N = a.n_paths;
+    const uint64_t total = N * (uint64_t)a.n_replicates;
+    const bool sobol = p->spec.rng == RNG_SOBOL;
+    const bool xorm = sobol && p->spec.scramble == SCRAMBLE_XOR;
+    const uint64_t dims_needed = (uint64_t)(T - 1) * NI;
+    if (sobol && dims_needed > (uint64_t)kSobolMaxDims)
+        fail(SDE_ERR_UNSUPPORTED, "Sobol sequence needs " + std::to_string(dims_needed) +
+                                      " dimensions; the Joe-Kuo table has " + std::to_string(kSobolMaxDims));
+    if (sobol && !xorm && a.path_offset + total + 5 > (1ull << 32))
+        fail(SDE_ERR_UNSUPPORTED, "Sobol point index beyond 2^32");
+    if (xorm && N > (1ull << 32)) fail(SDE_ERR_UNSUPPORTED, "more than 2^32 Sobol points per replicate");
+    const int block = p->spec.block;
+    const uint64_t gx = (N + block - 1) / block;
+    if (gx > 0x7fffffffull) fail(SDE_ERR_INVALID, "too many paths for one launch");
+
+    // output slots
+    std::vector<int32_t> slots;
+    switch (p->output) {
+    case SDE_OUT_FULL:
+        for (int t = 0; t < T; ++t) slots.push_back(t);
+        break;
+    case SDE_OUT_CHECKPOINTS:
+        for (int k = 0; k < a.n_checkpoints; ++k) {
+            int t = a.checkpoints[k];
+            if (t < 0 || t >= T) fail(SDE_ERR_INVALID, "checkpoint index out of range");
+            if (!slots.empty() && t <= slots.back()) fail(SDE_ERR_INVALID, "checkpoints must be increasing");
+            slots.push_back(t);
+        }
+        break;
+    case SDE_OUT_TERMINAL:
+        slots.push_back(T - 1);
+        break;
+    default:
+        break;
+    }
+
+    auto r = std::make_unique<sde_result>();
+    r->plan = p;
+    r->n_paths = N;
+    r->n_rep = a.n_replicates;
+    r->n_out = (int)slots.size();
+    r->P = P;
+    r->K = (int)p->spec.payoffs.size();
+    r->elem = p->spec.precision == PREC_FP32 ? 4 : 8;
+    r->scen_base = a.path_offset;
+    r->slot_tidx = slots;
+    for (int t : slots) r->slot_times.push_back(a.times[t]);
+    r->stream = (cudaStream_t)a.stream;
+
+    Loaded& L = ensure_loaded(p);
+
+    // stage the small inputs in one pinned block and copy them in one go
+    const int Tm1 = std::max(1, T - 1);
+    const size_t nd = (size_t)T + 2 * Tm1 + std::max(1, P) + std::max<size_t>(1, u.params.size());
+    const size_t nf = (size_t)T + 2 * Tm1;
+    const size_t bytes = nd * 8 + nf * 4 + (size_t)T * 4 + 64;
+    r->stage = HBuf(bytes);
+    char* h = r->stage.as<char>();
+    double* hd = (double*)h;
+    double* h_times = hd;
+    double* h_dts = h_times + T;
+    double* h_sdts = h_dts + Tm1;
+    double* h_x0 = h_sdts + Tm1;
+    double* h_par = h_x0 + std::max(1, P);
+    float* hf = (float*)(hd + nd);
+    float* h_times_f = hf;
+    float* h_dts_f = hf + T;
+    float* h_sdts_f = h_dts_f + Tm1;
+    int32_t* h_tidx = (int32_t*)(hf + nf);
+    for (int t = 0; t < T; ++t) {
+        h_times[t] = a.times[t];
+        h_times_f[t] = (float)a.times[t];
+        h_tidx[t] = -1;
+    }
+    for (int t = 0; t + 1 < T; ++t) {
+        h_dts[t] = a.times[t + 1] - a.times[t];
+        h_sdts[t] = std::sqrt(a.times[t + 1] - a.times[t]);
+        h_dts_f[t] = (float)h_dts[t];
+        h_sdts_f[t] = (float)h_sdts[t];
+    }
+    for (int q = 0; q < std::max(1, P); ++q) h_x0[q] = (a.x0 && q < a.n_x0) ? a.x0[q] : 0.0;
+    for (size_t k = 0; k < u.params.size(); ++k) h_par[k] = a.params[k];
+    for (size_t s = 0; s < slots.size(); ++s) h_tidx[slots[s]] = (int32_t)s;
+    r->args_dev = DBuf(bytes);
+    cuda_check(cudaMemcpyAsync(r->args_dev.p, h, bytes, cudaMemcpyHostToDevice, r->stream), "stage inputs");
+    char* d = r->args_dev.as<char>();
+    auto dptr = [&](const void* hp) { return d + ((const char*)hp - h); };
+
+    sde_args A;
+    std::memset(&A, 0, sizeof A);
+    A.times = (const double*)dptr(h_times);
+    A.dts = (const double*)dptr(h_dts);
+    A.sqrt_dts = (const double*)dptr(h_sdts);
+    A.times_f = (const float*)dptr(h_times_f);
+    A.dts_f = (const float*)dptr(h_dts_f);
+    A.sqrt_dts_f = (const float*)dptr(h_sdts_f);
+    A.x0 = (const double*)dptr(h_x0);
+    A.params = (const double*)dptr(h_par);
+    A.out_tidx = (const int*)dptr(h_tidx);
+    A.n_paths = N;
+    A.path_base = a.path_offset;
+    A.seed = a.seed;
+    A.T = T;
+    A.n_out = r->n_out;
+    A.n_rep = a.n_replicates;
+
+    if (sobol) {
+        SobolTables& st = sobol_tables(r->stream);
+        A.sobol_v = st.V.as<sde_u32>();
+        A.sobol_vt = st.VT.as<sde_u32>();
+        A.sobol_lo = st.LO.as<sde_u32>();
+        A.sobol_dims = st.dims;
+        if (xorm) {
+            const int stride = (int)((dims_needed + 31) / 32 * 32);
+            r->masks = DBuf((size_t)stride * a.n_replicates * 4 + 4);
+            cuda_check(launch_make_xor_masks(r->masks.as<sde_u32>(), a.n_replicates, stride, a.seed, r->stream),
+                       "XOR masks");
+            A.masks = r->masks.as<sde_u32>();
+            A.mask_stride = stride;
+        }
+    }
+
+    // filtration buffer
+    const size_t out_bytes = (size_t)r->n_out * P * N * a.n_replicates * r->elem;
+    if (r->n_out > 0 && P > 0 && N > 0) {
+        if (a.device_out) {
+            if (a.device_out_bytes < out_bytes)
+                fail(SDE_ERR_INVALID, "device_out is smaller than the filtration (" + std::to_string(out_bytes) + " bytes)");
+            r->out_ptr = a.device_out;
+        } else {
+            r->out = DBuf(out_bytes);
+            r->out_ptr = r->out.p;
+        }
+    }
+    A.out = r->out_ptr;
+
+    if (r->K > 0) {
+        r->partials = DBuf((size_t)a.n_replicates * gx * r->K * 4 * 8 + 8);
+        r->est_dev = DBuf((size_t)a.n_replicates * r->K * 2 * 8);
+        r->est_host = HBuf((size_t)a.n_replicates * r->K * 2 * 8);
+        A.partials = r->partials.as<double>();
+    }
+
+    if (N > 0 && T >= 1) {
+        void* kargs[] = {&A};
+        cuda_check(cudaLaunchKernel((const void*)L.fwd, dim3((unsigned)gx, (unsigned)a.n_replicates),
+                                    dim3(block), kargs, 0, r->stream),
+                   "step kernel launch");
+        if (r->K > 0) {
+            cuda_check(launch_reduce_partials(r->partials.as<double>(), (int)gx, r->K, a.n_replicates,
+                                              r->est_dev.as<double>(), r->stream),
+                       "estimator reduction");
+            cuda_check(cudaMemcpyAsync(r->est_host.p, r->est_dev.p, (size_t)a.n_replicates * r->K * 2 * 8,
+                                       cudaMemcpyDeviceToHost, r->stream),
+                       "estimates D2H");
+        }
+    } else if (r->K > 0) {
+        std::memset(r->est_host.p, 0, (size_t)a.n_replicates * r->K * 2 * 8);
+    }
+    cuda_check(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventRecord(r->done, r->stream), "cudaEventRecord");
+    return r.release();
+}
+
+static void wait(sde_result* r) {
+    if (r->waited) return;
+    cuda_check(cudaEventSynchronize(r->done), "kernel execution");
+    r->waited = true;
+}
+
+}  // namespace sde
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+using namespace sde;
+
+extern "C" {
+
+int32_t sde_abi_version(void) { return SDE_ABI_VERSION; }
+
+int sde_last_error(char* buf, size_t n) {
+    if (!buf || n == 0) return SDE_ERR_INVALID;
+    std::snprintf(buf, n, "%s", g_last_error.c_str());
+    return SDE_OK;
+}
+
+void sde_options_init(sde_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->struct_size = sizeof *o;
+    o->scheme = SDE_SCHEME_EULER;
+    o->rng = SDE_RNG_PSEUDO;
+    o->scramble = SDE_SCRAMBLE_SHIFT;
+    o->precision = SDE_FP64;
+    o->semantics = SDE_SEM_REFERENCE;
+    o->output = SDE_OUT_FULL;
+}
+
+void sde_run_args_init(sde_run_args* a) {
+    if (!a) return;
+    std::memset(a, 0, sizeof *a);
+    a->struct_size = sizeof *a;
+    a->n_replicates = 1;
+}
+
+static std::vector<std::string> strs(const char* const* s, int n) {
+    std::vector<std::string> v;
+    for (int i = 0; i < n; ++i) {
+        if (!s || !s[i]) fail(SDE_ERR_INVALID, "NULL string");
+        v.emplace_back(s[i]);
+    }
+    return v;
+}
+
+int sde_plan_create(const char* const* equations, int32_t n_equations, const char* const* param_names,
+                    int32_t n_params, const char* const* payoffs, int32_t n_payoffs,
+                    const sde_options* opts, sde_plan** out_plan) {
+    return guarded([&] {
+        if (!out_plan) fail(SDE_ERR_INVALID, "out_plan is NULL");
+        *out_plan = nullptr;
+        if (n_equations < 0 || n_params < 0 || n_payoffs < 0) fail(SDE_ERR_INVALID, "negative count");
+        sde_options o;
+        sde_options_init(&o);
+        if (opts) {
+            if (opts->struct_size != sizeof(sde_options)) fail(SDE_ERR_INVALID, "sde_options.struct_size mismatch");
+            o = *opts;
+        }
+        *out_plan = plan_create(strs(equations, n_equations), strs(param_names, n_params),
+                                strs(payoffs, n_payoffs), o);
+    });
+}
+
+int sde_plan_destroy(sde_plan* p) {
+    return guarded([&] {
+        if (!p) return;
+        for (auto& kv : p->loaded)
+            if (kv.second.lib) {
+                int cur = 0;
+                cudaGetDevice(&cur);
+                cudaSetDevice(kv.first);
+                cudaLibraryUnload(kv.second.lib);
+                cudaSetDevice(cur);
+            }
+        delete p;
+    });
+}
+
+int sde_plan_n_processes(const sde_plan* p, int32_t* n) {
+    return guarded([&] {
+        if (!p || !n) fail(SDE_ERR_INVALID, "NULL argument");
+        *n = p->u.n_processes();
+    });
+}
+
+int sde_plan_n_stochastic(const sde_plan* p, int32_t* n) {
+    return guarded([&] {
+        if (!p || !n) fail(SDE_ERR_INVALID, "NULL argument");
+        *n = p->u.n_stochastic();
+    });
+}
+
+int sde_plan_process_name(const sde_plan* p, int32_t i, char* buf, size_t n) {
+    return guarded([&] {
+        if (!p || !buf) fail(SDE_ERR_INVALID, "NULL argument");
+        if (i < 0 || i >= p->u.n_processes()) fail(SDE_ERR_INVALID, "process index out of range");
+        std::snprintf(buf, n, "%s", p->u.procs[i].name.c_str());
+    });
+}
+
+int sde_plan_process_index(const sde_plan* p, const char* name, int32_t* index) {
+    return guarded([&] {
+        if (!p || !name || !index) fail(SDE_ERR_INVALID, "NULL argument");
+        *index = p->u.process_index(name);
+    });
+}
+
+int sde_plan_stochastic_token(const sde_plan* p, int32_t i, char* buf, size_t n) {
+    return guarded([&] {
+        if (!p || !buf) fail(SDE_ERR_INVALID, "NULL argument");
+        if (i < 0 || i >= p->u.n_stochastic()) fail(SDE_ERR_INVALID, "stochastic index out of range");
+        std::snprintf(buf, n, "%s", p->u.tokens[i].c_str());
+    });
+}
+
+int sde_plan_source(const sde_plan* p, char* buf, size_t n, size_t* needed) {
+    return guarded([&] {
+        if (!p) fail(SDE_ERR_INVALID, "NULL plan");
+        if (needed) *needed = p->source.size() + 1;
+        if (buf && n) std::snprintf(buf, n, "%s", p->source.c_str());
+    });
+}
+
+int sde_run(sde_plan* p, const sde_run_args* a, sde_result** out) {
+    return guarded([&] {
+        if (!p || !a || !out) fail(SDE_ERR_INVALID, "NULL argument");
+        if (a->struct_size != sizeof(sde_run_args)) fail(SDE_ERR_INVALID, "sde_run_args.struct_size mismatch");
+        *out = nullptr;
+        *out = run(p, *a);
+    });
+}
+
+int sde_simulate(const char* const* equations, int32_t n_equations, const double* times, int32_t n_times,
+                 const char* const* init_names, const double* init_values, int32_t n_init,
+                 uint64_t n_scenarios, const char* scheme, const char* rng_method, uint64_t seed,
+                 int32_t has_seed, sde_result** out) {
+    return guarded([&] {
+        if (!out || !scheme || !rng_method) fail(SDE_ERR_INVALID, "NULL argument");
+        *out = nullptr;
+        sde_options o;
+        sde_options_init(&o);
+        if (std::strcmp(scheme, "euler") == 0) o.scheme = SDE_SCHEME_EULER;
+        else if (std::strcmp(scheme, "runge-kutta") == 0) o.scheme = SDE_SCHEME_RK;
+        else fail(SDE_ERR_INVALID, std::string("unknown scheme '") + scheme + "'");
+        o.rng = std::strcmp(rng_method, "sobol") == 0 ? SDE_RNG_SOBOL : SDE_RNG_PSEUDO;
+        std::shared_ptr<sde_plan> plan(plan_create(strs(equations, n_equations), {}, {}, o));
+        std::vector<double> x0(std::max(1, plan->u.n_processes()), 0.0);
+        for (int k = 0; k < n_init; ++k) {
+            int idx = plan->u.process_index(init_names[k]);
+            if (idx >= 0) x0[idx] = init_values[k];
+        }
+        if (!has_seed) {
+            std::random_device rd;
+            seed = ((uint64_t)rd() << 32) ^ rd();
+        }
+        sde_run_args a;
+        sde_run_args_init(&a);
+        a.times = times;
+        a.n_times = n_times;
+        a.x0 = x0.data();
+        a.n_x0 = plan->u.n_processes();
+        a.n_paths = n_scenarios;
+        a.seed = seed;
+        sde_result* r = run(plan.get(), a);
+        r->plan_keep = plan;
+        *out = r;
+    });
+}
+
+int sde_result_destroy(sde_result* r) {
+    return guarded([&] {
+        if (!r) return;
+        if (r->done) {
+            cudaEventSynchronize(r->done);
+            cudaEventDestroy(r->done);
+        }
+        delete r;
+    });
+}
+
+int sde_result_wait(sde_result* r) {
+    return guarded([&] {
+        if (!r) fail(SDE_ERR_INVALID, "NULL result");
+        wait(r);
+    });
+}
+
+int sde_result_shape(const sde_result* r, uint64_t* n_paths, int32_t* n_out, int32_t* n_proc, int32_t* n_rep) {
+    return guarded([&] {
+        if (!r) fail(SDE_ERR_INVALID, "NULL result");
+        if (n_paths) *n_paths = r->n_paths;
+        if (n_out) *n_out = r->n_out;
+        if (n_proc) *n_proc = r->P;
+        if (n_rep) *n_rep = r->n_rep;
+    });
+}
+
+int sde_result_time_indices(const sde_result* r, int32_t* out) {
+    return guarded([&] {
+        if (!r || !out) fail(SDE_ERR_INVALID, "NULL argument");
+        std::copy(r->slot_tidx.begin(), r->slot_tidx.end(), out);
+    });
+}
+
+int sde_result_device_values(const sde_result* r, void** dptr, int32_t* elem) {
+    return guarded([&] {
+        if (!r || !dptr) fail(SDE_ERR_INVALID, "NULL argument");
+        *dptr = r->out_ptr;
+        if (elem) *elem = r->elem;
+    });
+}
+
+int sde_result_copy_values(sde_result* r, double* host, int32_t layout) {
+    return guarded([&] {
+        if (!r || !host) fail(SDE_ERR_INVALID, "NULL argument");
+        const size_t n = (size_t)r->n_rep * r->n_paths * r->n_out * r->P;
+        if (n == 0) return;
+        if (!r->out_ptr) fail(SDE_ERR_INVALID, "the plan stores no filtration");
+        if (layout == SDE_LAYOUT_DEVICE) {
+            wait(r);
+            if (r->elem == 8) {
+                cuda_check(cudaMemcpy(host, r->out_ptr, n * 8, cudaMemcpyDeviceToHost), "D2H");
+            } else {
+                std::vector<float> tmp(n);
+                cuda_check(cudaMemcpy(tmp.data(), r->out_ptr, n * 4, cudaMemcpyDeviceToHost), "D2H");
+                for (size_t i = 0; i < n; ++i) host[i] = tmp[i];
+            }
+            return;
+        }
+        if (layout != SDE_LAYOUT_REFERENCE) fail(SDE_ERR_INVALID, "unknown layout");
+        DBuf val(n * 8);
+        cuda_check(launch_long_export(r->out_ptr, r->elem, r->n_paths, r->n_out, r->P, r->n_rep, nullptr,
+                                      0, nullptr, nullptr, nullptr, val.as<double>(), r->stream),
+                   "export");
+        cuda_check(cudaMemcpyAsync(host, val.p, n * 8, cudaMemcpyDeviceToHost, r->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(r->stream), "D2H");
+        r->waited = true;
+    });
+}
+
+int sde_result_copy_long(sde_result* r, int32_t* scen, double* time, int32_t* proc, double* value) {
+    return guarded([&] {
+        if (!r) fail(SDE_ERR_INVALID, "NULL result");
+        const size_t n = (size_t)r->n_rep * r->n_paths * r->n_out * r->P;
+        if (n == 0) return;
+        if (!r->out_ptr) fail(SDE_ERR_INVALID, "the plan stores no filtration");
+        DBuf st(std::max<size_t>(1, r->slot_times.size()) * 8);
+        cuda_check(cudaMemcpyAsync(st.p, r->slot_times.data(), r->slot_times.size() * 8, cudaMemcpyHostToDevice,
+                                   r->stream),
+                   "slot times");
+        DBuf ds(scen ? n * 4 : 0), dt(time ? n * 8 : 0), dp(proc ? n * 4 : 0), dv(value ? n * 8 : 0);
+        cuda_check(launch_long_export(r->out_ptr, r->elem, r->n_paths, r->n_out, r->P, r->n_rep,
+                                      st.as<double>(), r->scen_base, ds.as<int32_t>(), dt.as<double>(),
+                                      dp.as<int32_t>(), dv.as<double>(), r->stream),
+                   "long export");
+        if (scen) cuda_check(cudaMemcpyAsync(scen, ds.p, n * 4, cudaMemcpyDeviceToHost, r->stream), "D2H");
+        if (time) cuda_check(cudaMemcpyAsync(time, dt.p, n * 8, cudaMemcpyDeviceToHost, r->stream), "D2H");
+        if (proc) cuda_check(cudaMemcpyAsync(proc, dp.p, n * 4, cudaMemcpyDeviceToHost, r->stream), "D2H");
+        if (value) cuda_check(cudaMemcpyAsync(value, dv.p, n * 8, cudaMemcpyDeviceToHost, r->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(r->stream), "D2H");
+        r->waited = true;
+    });
+}
+
+int sde_result_estimates(sde_result* r, double* sum, double* sumsq) {
+    return guarded([&] {
+        if (!r) fail(SDE_ERR_INVALID, "NULL result");
+        wait(r);
+        const double* e = r->est_host.as<double>();
+        for (int i = 0; i < r->n_rep * r->K; ++i) {
+            if (sum) sum[i] = e[2 * i];
+            if (sumsq) sumsq[i] = e[2 * i + 1];
+        }
+    });
+}
+
+int sde_kat_chacha8_u64(uint64_t seed, uint64_t first, uint64_t n, uint64_t* host_out) {
+    return guarded([&] {
+        if (!host_out && n) fail(SDE_ERR_INVALID, "NULL output");
+        DBuf d(n * 8);
+        cuda_check(launch_kat_chacha8(seed, first, n, d.as<sde_u64>(), nullptr), "chacha8 kernel");
+        cuda_check(cudaMemcpy(host_out, d.p, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    });
+}
+
+int sde_kat_sobol_points(int32_t dims, uint64_t first, uint64_t n, uint32_t* host_out) {
+    return guarded([&] {
+        if (dims < 1 || dims > kSobolMaxDims) fail(SDE_ERR_INVALID, "dims out of range");
+        if (first + n > (1ull << 32)) fail(SDE_ERR_UNSUPPORTED, "Sobol index beyond 2^32");
+        SobolTables& st = sobol_tables(nullptr);
+        DBuf d(n * dims * 4);
+        cuda_check(launch_kat_sobol(st.V.as<sde_u32>(), dims, first, n, d.as<sde_u32>(), nullptr), "sobol kernel");
+        cuda_check(cudaMemcpy(host_out, d.p, n * dims * 4, cudaMemcpyDeviceToHost), "D2H");
+    });
+}
+
+int sde_kat_icdf(const double* host_p, uint64_t n, double* host_out) {
+    return guarded([&] {
+        DBuf dp(n * 8), dq(n * 8);
+        cuda_check(cudaMemcpy(dp.p, host_p, n * 8, cudaMemcpyHostToDevice), "H2D");
+        cuda_check(launch_kat_icdf(dp.as<double>(), n, dq.as<double>(), nullptr), "icdf kernel");
+        cuda_check(cudaMemcpy(host_out, dq.p, n * 8, cudaMemcpyDeviceToHost), "D2H");
+    });
+}
+
+int sde_sobol_directions(int32_t dims, uint32_t* host_out) {
+    return guarded([&] {
+        if (dims < 1 || dims > kSobolMaxDims) fail(SDE_ERR_INVALID, "dims out of range");
+        if (!host_out) fail(SDE_ERR_INVALID, "NULL output");
+        sobol_directions_host(dims, host_out);
+    });
+}
+
+int sde_probe_sfu_peak(double* ops) {
+    return guarded([&] {
+        if (!ops) fail(SDE_ERR_INVALID, "NULL output");
+        cuda_check(run_sfu_probe(ops), "SFU probe");
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+"""Host side of the engine without a GPU: the C ABI library, the equation
+front end, the lowering (NVRTC compiles for sm_103a on the CPU) and the
+error behaviour of the drop-in."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import EXAMPLE_GBM, EXAMPLE_PY, EXAMPLE_RS, GBM, HESTON, OU, ROOT
+
+
+def _declared_symbols():
+    with open(os.path.join(ROOT, "include", "sdegpu.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sde_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(engine):
+    from sde_sim_rs import _native as N
+    lib = C.CDLL(N.LIB_PATH)
+    names = _declared_symbols()
+    assert len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+    # and the binding declares a signature for each of them
+    assert set(names) == set(N.SIGNATURES)
+    assert lib.sde_abi_version() == 1
+
+
+def test_struct_sizes_match_header(engine):
+    from sde_sim_rs import _native as N
+    o = N.Options()
+    N.lib().sde_options_init(C.byref(o))
+    assert o.struct_size == C.sizeof(N.Options)
+    a = N.RunArgs()
+    N.lib().sde_run_args_init(C.byref(a))
+    assert a.struct_size == C.sizeof(N.RunArgs) and a.n_replicates == 1
+
+
+@pytest.mark.parametrize("eqs", [GBM, EXAMPLE_RS, EXAMPLE_PY, EXAMPLE_GBM, HESTON, OU])
+def test_front_end_matches_oracle(engine, oracle, eqs):
+    p = engine.Plan(eqs)
+    u = oracle.Universe(eqs)
+    assert p.process_names == u.process_names
+    assert p.stochastic_tokens == u.stochastic_tokens
+
+
+@pytest.mark.parametrize("scheme", ["euler", "runge-kutta"])
+@pytest.mark.parametrize("rng,scramble", [("pseudo", "shift"), ("sobol", "shift"), ("sobol", "xor")])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("semantics", ["reference", "textbook"])
+def test_lowering_compiles(engine, scheme, rng, scramble, precision, semantics):
+    p = engine.Plan(EXAMPLE_PY, scheme=scheme, rng=rng, scramble=scramble, precision=precision,
+                    semantics=semantics, payoffs=["max(X1 - 100, 0)", "X0"])
+    src = p.source
+    assert "__global__" in src and "sde_step_" in src
+    if precision == "fp32":
+        # FP32 stepping: no double arithmetic in the step body
+        body = src.split("for (int t0 = 0;")[1].split("double f[")[0]
+        assert "double" not in body
+
+
+def test_fasteval_operators_compile(engine):
+    # '=' may not appear in an equation (the reference splits on it), so the
+    # comparisons that contain one are exercised through a payoff
+    expr = ("(abs(X) + sign(X) + int(X) + ceil(X) + floor(X) + round(X) + round(0.5, X) + log(X)"
+            " + log(2, X) + e() + pi() + sin(X) + cos(X) + tan(X) + atan(X) + sinh(X) + tanh(X)"
+            " + (X > 1) + (X < 1) + (X && 1)"
+            " + (X || 0) + !X + X % 3 + X ^ 1.5 + -X ^ 2 + min(X, 1, 2) + max(X, t) + sqrt(X) + exp(-X))")
+    for prec in ("fp64", "fp32"):
+        engine.Plan([f"dX = {expr} * dt + (0.1) * dW1"], precision=prec,
+                    payoffs=["(X >= 1) + (X <= 1) + (X == 1) + (X != 1)"])
+    with pytest.raises(ValueError, match="Missing '='"):
+        engine.Plan(["dX = (X == 1) * dt"])
+
+
+@pytest.mark.parametrize("eq,msg", [
+    ("dX = (0.1 * X) * dt = 3", "Missing '='"),
+    ("dX = (0.1 * X * dt", "Unbalanced parentheses in coefficient"),
+    ("dX = (0.1 * X) * dZ1", "Unknown incrementor type: dZ1"),
+    ("dX = (0.1 * ) * dt", "Math error in coefficient"),
+    ("dX = (0.1) * dN1(X", "Unbalanced parentheses in dN intensity"),
+    ("dX = (0.1 * Y) * dt", "Unknown variable 'Y'"),
+])
+def test_parse_errors_raise_value_error(engine, eq, msg):
+    with pytest.raises(ValueError, match=re.escape(msg)):
+        engine.Plan([eq])
+
+
+def test_simulate_argument_errors(engine):
+    with pytest.raises(ValueError, match="scenarios must be a positive integer"):
+        engine.simulate(GBM, [0.0, 1.0], 0, {"X": 1.0})
+    with pytest.raises(ValueError, match="unknown scheme"):
+        engine.simulate(GBM, [0.0, 1.0], 1, {"X": 1.0}, scheme="milstein")
+    with pytest.raises(ValueError, match="Failed to parse equations"):
+        engine.simulate(["dX = (X * dt"], [0.0, 1.0], 1, {"X": 1.0})
+
+
+def test_params_are_declared_names(engine):
+    p = engine.Plan(["dX = (mu * X) * dt + (sigma * X) * dW1"], params=["mu", "sigma"])
+    assert "PR0" in p.source and "PR1" in p.source
+    with pytest.raises(ValueError, match="name of a process"):
+        engine.Plan(["dX = (X) * dt"], params=["X"])
+
+
+def test_host_sobol_directions_match_oracle(engine, oracle):
+    from sde_sim_rs import _native as N
+    dims = 21201
+    V = np.zeros((dims, 32), dtype=np.uint32)
+    N.check(N.lib().sde_sobol_directions(dims, V.ctypes.data))
+    assert np.array_equal(V, oracle.sobol_directions(dims))
+
+
+def test_sobol_dimension_limit_message(engine):
+    p = engine.Plan(GBM, rng="sobol")
+    # 21201 dimensions is the Joe-Kuo table: one more step than that fails
+    # before touching a device
+    with pytest.raises(Exception, match="Joe-Kuo table has 21201"):
+        p.run(np.arange(21203, dtype=np.float64), {"X": 1.0}, 4)

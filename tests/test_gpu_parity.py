@@ -1,0 +1,284 @@
+"""GPU parity: the lowered sm_103a kernels through the C ABI against the CPU
+oracle on the same seeded inputs.
+
+Bars: integer RNG work (ChaCha8 words, Sobol points, scramble bits) is
+bit-exact; FP64 paths agree within 1e-12 relative (|gpu-ref| <= 1e-12 *
+max(|ref|, 1)); FP32 stepping is compared with the FP64 oracle on the same
+random inputs, by per-path relative error (stated) and by estimator means
+within 3 standard errors.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import EXAMPLE_GBM, EXAMPLE_PY, EXAMPLE_RS, GBM, GOLDEN, HESTON, OU
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12
+THREADS = os.cpu_count() or 1
+
+
+def close64(gpu, ref):
+    err = np.abs(gpu - ref) / np.maximum(np.abs(ref), 1.0)
+    bad = ~(err <= FP64_RTOL) & ~(np.isnan(gpu) & np.isnan(ref))
+    return float(np.nanmax(err)) if err.size else 0.0, int(bad.sum())
+
+
+# ---------------------------------------------------------------- KAT kernels
+
+@pytest.mark.parametrize("seed", [0, 42, 2**63 + 11, 2**64 - 1])
+def test_kat_chacha8_bit_exact(engine, oracle, seed):
+    from sde_sim_rs import _native as N
+    for first, n in ((0, 1000), (12345, 333)):
+        out = np.zeros(n, dtype=np.uint64)
+        N.check(N.lib().sde_kat_chacha8_u64(seed, first, n, out.ctypes.data))
+        assert np.array_equal(out, oracle.chacha8_u64(seed, first, n))
+
+
+def test_kat_sobol_bit_exact(engine, oracle):
+    from sde_sim_rs import _native as N
+    g = np.load(os.path.join(GOLDEN, "sobol_scipy.npz"))
+    out = np.zeros((256, 64), dtype=np.uint32)
+    N.check(N.lib().sde_kat_sobol_points(64, 0, 256, out.ctypes.data))
+    assert np.array_equal(out, g["first256_d64"])
+    out = np.zeros((64, 8), dtype=np.uint32)
+    N.check(N.lib().sde_kat_sobol_points(8, 1000000, 64, out.ctypes.data))
+    assert np.array_equal(out, g["at1e6_d8"])
+    out = np.zeros((100, 8192), dtype=np.uint32)
+    N.check(N.lib().sde_kat_sobol_points(8192, 2**20 - 50, 100, out.ctypes.data))
+    assert np.array_equal(out, oracle.sobol_points(8192, 2**20 - 50, 100))
+
+
+def test_kat_icdf(engine, oracle):
+    from sde_sim_rs import _native as N
+    with open(os.path.join(GOLDEN, "icdf.json")) as f:
+        g = json.load(f)
+    rng = np.random.default_rng(1)
+    p = np.concatenate([np.array(g["p"]), rng.random(10000)])
+    out = np.zeros_like(p)
+    N.check(N.lib().sde_kat_icdf(p.ctypes.data, len(p), out.ctypes.data))
+    ref = np.array([oracle.icdf_as26(float(x)) for x in p])
+    assert np.max(np.abs(out - ref) / np.maximum(np.abs(ref), 1e-3)) < 1e-14
+
+
+# ---------------------------------------------------------------- FP64 parity
+
+def test_c0_gbm_full_filtration(engine, oracle):
+    """The reference's plain configuration: GBM, Euler, 252 steps, 10,000
+    paths, pseudo-random seed 42, FP64, all 253 time points."""
+    times = [i / 252 for i in range(253)]
+    plan = engine.Plan(GBM, scheme="euler", rng="pseudo", precision="fp64", output="full")
+    gpu = plan.run(times, {"X": 100.0}, 10000, seed=42).values("reference")[0]
+    ref = oracle.Universe(GBM).simulate(times, {"X": 100.0}, 0, 10000, seed=42, threads=THREADS)
+    err, nbad = close64(gpu, ref)
+    assert nbad == 0, err
+    xt = gpu[:, -1, 0]
+    m, v = 100 * math.exp(0.05), 100 ** 2 * math.exp(0.1) * (math.exp(0.04) - 1)
+    assert abs(xt.mean() - m) < 4 * math.sqrt(v / len(xt))
+    assert abs(xt.std() / math.sqrt(v) - 1) < 0.05
+
+
+CASES = {
+    "gbm": (GBM, {"X": 100.0}),
+    "example_rs": (EXAMPLE_RS, {"X1": 100.0, "X2": 0.0}),
+    "example_py": (EXAMPLE_PY, {"X0": 0.5, "X1": 100.0, "X2": 0.0}),
+    "example_gbm": (EXAMPLE_GBM, {"X1": 1.0}),
+    "heston": (HESTON, {"S": 100.0, "v": 0.04}),
+    "ou": (OU, {"X": 0.0}),
+}
+RNGS = {"pseudo": ("pseudo", "shift"), "sobol_shift": ("sobol", "shift"), "sobol_xor": ("sobol", "xor")}
+
+
+def _oracle_cfg(oracle, scheme, rng, semantics):
+    r, s = RNGS[rng]
+    return dict(scheme=oracle.RK if scheme == "runge-kutta" else oracle.EULER,
+                rng=oracle.SOBOL if r == "sobol" else oracle.PSEUDO,
+                scramble=oracle.XOR if s == "xor" else oracle.SHIFT,
+                semantics=oracle.TEXTBOOK if semantics == "textbook" else oracle.REFERENCE)
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("scheme", ["euler", "runge-kutta"])
+@pytest.mark.parametrize("rng", list(RNGS))
+@pytest.mark.parametrize("semantics", ["reference", "textbook"])
+def test_fp64_paths_match_oracle(engine, oracle, case, scheme, rng, semantics):
+    eqs, init = CASES[case]
+    times = np.linspace(0.0, 2.0, 41) if case != "example_rs" else np.arange(0.0, 4.0, 0.1)
+    n, seed = 300, 20240607
+    r, s = RNGS[rng]
+    plan = engine.Plan(eqs, scheme=scheme, rng=r, scramble=s, precision="fp64", semantics=semantics)
+    gpu = plan.run(times, init, n, seed=seed).values("reference")[0]
+    ref = oracle.Universe(eqs).simulate(times, init, 0, n, seed=seed, n_per_replicate=n,
+                                        threads=THREADS, **_oracle_cfg(oracle, scheme, rng, semantics))
+    err, nbad = close64(gpu, ref)
+    if any("dN" in e for e in eqs):
+        # a jump count may flip when the FP64 intensity differs in its last
+        # bit at a CDF boundary; such a path then differs from that step on
+        paths_bad = np.unique(np.argwhere(np.abs(gpu - ref) > FP64_RTOL * np.maximum(np.abs(ref), 1))[:, 0])
+        assert len(paths_bad) <= 1, (err, paths_bad)
+    else:
+        assert nbad == 0, err
+
+
+def test_replicates_and_offsets_are_scenario_ranges(engine, oracle):
+    times = np.linspace(0, 1, 17)
+    plan = engine.Plan(EXAMPLE_PY, scheme="runge-kutta")
+    init = {"X0": 0.5, "X1": 100.0}
+    a = plan.run(times, init, 50, replicates=3, seed=5).values("reference")
+    b = plan.run(times, init, 40, seed=5, path_offset=110).values("reference")[0]
+    ref = oracle.Universe(EXAMPLE_PY).simulate(times, init, 0, 150, scheme=oracle.RK, seed=5)
+    assert close64(a.reshape(150, 17, 3), ref)[1] == 0
+    assert close64(b, ref[110:150])[1] == 0
+
+
+def test_xor_replicates_match_oracle(engine, oracle):
+    times = np.linspace(0, 1, 65)
+    plan = engine.Plan(HESTON, rng="sobol", scramble="xor")
+    gpu = plan.run(times, {"S": 100.0, "v": 0.04}, 96, replicates=4, seed=7).values("reference")
+    ref = oracle.Universe(HESTON).simulate(times, {"S": 100.0, "v": 0.04}, 0, 4 * 96, rng=oracle.SOBOL,
+                                           scramble=oracle.XOR, seed=7, n_per_replicate=96)
+    assert close64(gpu.reshape(4 * 96, 65, 2), ref)[1] == 0
+
+
+def test_output_modes_are_slices_of_full(engine):
+    times = np.linspace(0, 1, 33)
+    full = engine.Plan(HESTON).run(times, {"S": 100.0, "v": 0.04}, 200, seed=3).values("reference")
+    ck = engine.Plan(HESTON, output="checkpoints").run(times, {"S": 100.0, "v": 0.04}, 200, seed=3,
+                                                       checkpoints=[0, 8, 31, 32])
+    assert ck.time_indices.tolist() == [0, 8, 31, 32]
+    assert np.array_equal(ck.values("reference"), full[:, :, [0, 8, 31, 32], :])
+    term = engine.Plan(HESTON, output="terminal").run(times, {"S": 100.0, "v": 0.04}, 200, seed=3)
+    assert np.array_equal(term.values("reference")[:, :, 0, :], full[:, :, -1, :])
+    dev = term.values("device")
+    assert dev.shape == (1, 1, 2, 200)
+    assert np.array_equal(dev[0, 0].T, full[0, :, -1, :])
+
+
+def test_long_format_rows(engine, oracle):
+    times = np.linspace(0, 1, 5)
+    plan = engine.Plan(EXAMPLE_PY)
+    res = plan.run(times, {"X0": 0.5, "X1": 100.0}, 7, seed=1, path_offset=3)
+    cols = res.long()
+    n = 7 * 5 * 3
+    assert cols["scenario"].tolist() == [3 + s for s in range(7) for _ in range(5) for _ in range(3)]
+    assert cols["time"].tolist() == [t for _ in range(7) for t in times for _ in range(3)]
+    assert cols["process"].tolist() == [p for _ in range(7 * 5) for p in range(3)]
+    ref = oracle.Universe(EXAMPLE_PY).simulate(times, {"X0": 0.5, "X1": 100.0}, 3, 10, seed=1)
+    assert close64(cols["value"], ref.reshape(n))[1] == 0
+
+
+def test_drop_in_simulate_frame(engine, oracle):
+    times = [i / 252 for i in range(253)]
+    fr = engine.simulate(GBM, times, 100, {"X": 100.0}, "pseudo", "euler", seed=42, output_format="numpy")
+    ref = oracle.Universe(GBM).simulate(times, {"X": 100.0}, 0, 100, seed=42)
+    assert len(fr) == 100 * 253
+    assert set(fr.keys()) == {"scenario", "time", "process_name", "value"}
+    assert fr["scenario"].dtype == np.int32 and fr["time"].dtype == np.float64
+    assert list(fr["process_name"][:3]) == ["X", "X", "X"]
+    assert close64(fr["value"], ref.reshape(-1))[1] == 0
+    # an unknown rng_method falls back to pseudo, as in the reference
+    fr2 = engine.simulate(GBM, times, 100, {"X": 100.0}, "quasi?", "euler", seed=42, output_format="numpy")
+    assert np.array_equal(fr2["value"], fr["value"])
+    fr3 = engine.simulate(GBM, times, 50, {"X": 100.0}, "sobol", "runge-kutta", seed=42, output_format="numpy")
+    ref3 = oracle.Universe(GBM).simulate(times, {"X": 100.0}, 0, 50, seed=42, rng=oracle.SOBOL,
+                                         scheme=oracle.RK)
+    assert close64(fr3["value"], ref3.reshape(-1))[1] == 0
+
+
+def test_estimators_fp64_match_oracle(engine, oracle):
+    times = np.linspace(0, 1, 51)
+    plan = engine.Plan(HESTON, payoffs=["max(S - 100, 0)", "S", "v"], output="none")
+    s, q = plan.run(times, {"S": 100.0, "v": 0.04}, 5000, replicates=2, seed=11).estimates()
+    u = oracle.Universe(HESTON)
+    for r in range(2):
+        for k, pay in enumerate(["max(S - 100, 0)", "S", "v"]):
+            rs, rq = u.estimate(times, {"S": 100.0, "v": 0.04}, r * 5000, (r + 1) * 5000, pay, seed=11,
+                                threads=THREADS)
+            assert abs(s[r, k] - rs) <= 1e-10 * max(abs(rs), 1)
+            assert abs(q[r, k] - rq) <= 1e-10 * max(abs(rq), 1)
+
+
+# ---------------------------------------------------------------- FP32 stepping
+
+@pytest.mark.parametrize("case", ["gbm", "heston", "ou", "example_py"])
+@pytest.mark.parametrize("scheme", ["euler", "runge-kutta"])
+@pytest.mark.parametrize("rng", list(RNGS))
+def test_fp32_against_fp64_oracle(engine, oracle, case, scheme, rng):
+    eqs, init = CASES[case]
+    times = np.linspace(0.0, 1.0, 65)
+    n, seed = 4000, 99
+    r, s = RNGS[rng]
+    plan = engine.Plan(eqs, scheme=scheme, rng=r, scramble=s, precision="fp32", output="terminal")
+    gpu = plan.run(times, init, n, seed=seed).values("reference")[0, :, 0, :]
+    ref = oracle.Universe(eqs).simulate(times, init, 0, n, seed=seed, n_per_replicate=n, full=False,
+                                        threads=THREADS, **_oracle_cfg(oracle, scheme, rng, "reference"))
+    scale = np.maximum(np.abs(ref), np.abs(ref).mean(axis=0, keepdims=True))
+    rel = np.abs(gpu - ref) / scale
+    # same random inputs: nearly every path agrees to FP32 accuracy
+    assert np.mean(rel < 1e-3) > 0.99, np.percentile(rel, [50, 99, 100])
+    for p in range(gpu.shape[1]):
+        se = ref[:, p].std() / math.sqrt(n)
+        assert abs(gpu[:, p].mean() - ref[:, p].mean()) <= 3 * se + 1e-12
+
+
+def test_heston_rqmc_estimator_fp32(engine, oracle):
+    """The Heston RQMC configuration at reduced size: XOR-scrambled Sobol,
+    16 replicates, FP32 stepping, FP64 estimator reduction."""
+    times = np.linspace(0.0, 1.0, 257)
+    n, reps = 4096, 16
+    plan = engine.Plan(HESTON, payoffs=["max(S - 100, 0)"], rng="sobol", scramble="xor",
+                       precision="fp32", output="none")
+    s, q = plan.run(times, {"S": 100.0, "v": 0.04}, n, replicates=reps, seed=7).estimates()
+    est = s[:, 0] / n
+    u = oracle.Universe(HESTON)
+    ref = []
+    for r in range(reps):
+        rs, _ = u.estimate(times, {"S": 100.0, "v": 0.04}, r * n, (r + 1) * n, "max(S - 100, 0)",
+                           rng=oracle.SOBOL, scramble=oracle.XOR, seed=7, n_per_replicate=n,
+                           threads=THREADS)
+        ref.append(rs / n)
+    ref = np.array(ref)
+    se = ref.std(ddof=1) / math.sqrt(reps)
+    # per replicate, same scrambled points: FP32 bias far below the RQMC error
+    assert np.max(np.abs(est - ref)) < 0.05 * se + 1e-4
+    assert abs(est.mean() - ref.mean()) < 3 * se
+
+
+# ---------------------------------------------------------------- edge cases
+
+def test_edge_cases(engine):
+    plan = engine.Plan(GBM, payoffs=["X"])
+    r = plan.run([0.0, 1.0], {"X": 1.0}, 0)
+    assert r.values().shape == (1, 0, 2, 1)
+    assert r.estimates()[0].tolist() == [[0.0]]
+    one = plan.run([0.5], {"X": 2.0}, 3).values()
+    assert one.shape == (1, 3, 1, 1) and np.all(one == 2.0)
+    rk = engine.Plan(["dX = (0.1 * X) * dt"], scheme="runge-kutta")
+    with pytest.raises(ValueError, match="RNG Index 0 out of bounds"):
+        rk.run([0.0, 1.0], {"X": 1.0}, 4)
+    assert rk.run([0.0], {"X": 1.0}, 4).values().shape == (1, 4, 1, 1)
+    with pytest.raises(ValueError, match="strictly increasing"):
+        plan.run([0.0, 1.0, 1.0], {"X": 1.0}, 4)
+    unknown = plan.run([0.0, 1.0], {"X": 1.0, "Q": 3.0}, 2).values()
+    missing = plan.run([0.0, 1.0], {}, 2).values()
+    assert np.all(missing == 0.0) and unknown.shape == (1, 2, 2, 1)
+
+
+def test_caller_owned_device_buffer(engine):
+    torch = pytest.importorskip("torch")
+    times = np.linspace(0, 1, 9)
+    plan = engine.Plan(HESTON, precision="fp32")
+    buf = torch.zeros(9 * 2 * 128, dtype=torch.float32, device="cuda")
+    r = plan.run(times, {"S": 100.0, "v": 0.04}, 128, seed=2, device_out=buf.data_ptr(),
+                 device_out_bytes=buf.numel() * 4)
+    ptr, elem = r.device_pointer()
+    assert ptr == buf.data_ptr() and elem == 4
+    r.wait()
+    ref = plan.run(times, {"S": 100.0, "v": 0.04}, 128, seed=2).values("device")[0]
+    assert np.array_equal(buf.cpu().numpy().reshape(9, 2, 128), ref.astype(np.float32))
+    with pytest.raises(ValueError, match="smaller than the filtration"):
+        plan.run(times, {"S": 100.0, "v": 0.04}, 128, device_out=buf.data_ptr(), device_out_bytes=16)
