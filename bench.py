@@ -163,15 +163,16 @@ def run_engine(args):
     from sde_sim_rs import _native as N
     import ctypes as C
 
+    npaths, reps = args.paths, args.reps
     plan = sde_sim_rs.Plan(HESTON, payoffs=[PAYOFF], rng="sobol", scramble="xor", precision="fp32",
                            output="none")
     T = times()
     stream = torch.cuda.current_stream()
-    seed = SEED + rank * REPS
+    seed = SEED + rank * reps
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    def one():
-        return plan.run(T, INIT, N_PATHS, replicates=REPS, seed=seed, stream=stream)
+    def one(p=plan, n=npaths):
+        return p.run(T, INIT, n, replicates=reps, seed=seed, stream=stream)
 
     for _ in range(args.warmup):
         one().estimates()
@@ -200,22 +201,47 @@ def run_engine(args):
         t = torch.tensor([ms_step], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_step = float(t.item())
-    path_steps = N_PATHS * REPS * STEPS_T
+    path_steps = npaths * reps * STEPS_T
     value = path_steps * world / (ms_step * 1e-3)
-    sums = np.array([r.estimates()[0][:, 0] for r in results[-1:]])[0]
-    price = float(sums.mean() / N_PATHS)
-    rep_means = sums / N_PATHS
-    price_se = float(rep_means.std(ddof=1) / math.sqrt(REPS))
+    sums = results[-1].estimates()[0][:, 0]
+    rep_means = sums / npaths
+    price = float(rep_means.mean())
+    price_se = float(rep_means.std(ddof=1) / math.sqrt(reps))
 
     # end to end through the public API: pinned H2D of the step's inputs,
     # kernel, D2H of the estimates, every step (host wall clock)
-    h2d = (len(T) * 3 + 2 * (len(T) - 1)) * 8 + 64
+    h2d = (len(T) * 3 + 2 * (len(T) - 1)) * 8 + len(T) * (4 + 4) + 64
     e2e_t = []
     for _ in range(max(3, args.steps // 2)):
         t0 = time.perf_counter()
-        plan.run(T, INIT, N_PATHS, replicates=REPS, seed=seed, stream=stream).estimates()
+        one().estimates()
         e2e_t.append(time.perf_counter() - t0)
     e2e_val = path_steps / statistics.median(e2e_t)
+
+    # the plain FP64 GPU path on the same scrambled inputs (a sample of the
+    # paths): its throughput and the FP32 estimate's deviation from it
+    fp64 = None
+    if args.fp64_paths:
+        p64 = sde_sim_rs.Plan(HESTON, payoffs=[PAYOFF], rng="sobol", scramble="xor", precision="fp64",
+                              output="none")
+        n64 = args.fp64_paths
+        one(p64, n64).estimates()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r64 = one(p64, n64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        r32 = one(plan, n64)
+        m64 = r64.estimates()[0][:, 0] / n64
+        m32 = r32.estimates()[0][:, 0] / n64
+        v64 = n64 * reps * STEPS_T / (ms64 * 1e-3)
+        bias = float(np.abs(m32 - m64).max())
+        se64 = float(m64.std(ddof=1) / math.sqrt(reps))
+        fp64 = {"value": v64, "unit": "path-steps/s", "sample": f"{n64} paths x {reps} replicates",
+                "estimate": float(m64.mean()),
+                "fp32_minus_fp64_max_abs_per_replicate": bias, "rqmc_se_at_sample": se64,
+                "equal_rmse_speedup": value / v64 * (1.0 if bias < se64 else (se64 / bias) ** 2)}
 
     # roofline: SFU bound; peak measured by a MUFU throughput probe
     peak = C.c_double()
@@ -230,12 +256,15 @@ def run_engine(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Sobol XOR scrambles)",
-            "config": {"workload": WORKLOAD, "paths": N_PATHS, "replicates": REPS, "steps": STEPS_T,
+            "config": {"workload": WORKLOAD if (npaths, reps) == (N_PATHS, REPS) else
+                       f"heston_rqmc_sobol_xor_{npaths}x{reps}_256steps (reduced)",
+                       "paths": npaths, "replicates": reps, "steps": STEPS_T,
                        "l2": "flushed (256 MiB write) between timed steps",
                        "estimate": price, "estimate_se_rqmc": price_se},
             "clocks": clk.summary(),
             "e2e": {"value": e2e_val, "unit": "path-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": REPS * 16},
+                    "d2h_bytes_per_step": reps * 16},
+            "fp64_gpu": fp64,
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value, "traffic": None,
@@ -258,6 +287,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--cpu-paths", type=int, default=1 << 17)
+    ap.add_argument("--paths", type=int, default=N_PATHS)
+    ap.add_argument("--reps", type=int, default=REPS)
+    ap.add_argument("--fp64-paths", type=int, default=1 << 14)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -74,7 +74,9 @@ typedef struct sde_options {
     int32_t semantics;      /* SDE_SEM_*           default REFERENCE       */
     int32_t output;         /* SDE_OUT_*           default FULL            */
     int32_t block_size;     /* threads per block, 0 = 256                  */
-    int32_t reserved[8];
+    int32_t ckpt_every;     /* adjoint plans: steps between checkpoints,
+                               0 = 19                                      */
+    int32_t reserved[7];
 } sde_options;
 
 typedef struct sde_run_args {
@@ -119,6 +121,21 @@ int sde_plan_create(const char* const* equations, int32_t n_equations,
                     const char* const* param_names, int32_t n_params,
                     const char* const* payoffs, int32_t n_payoffs,
                     const sde_options* opts, sde_plan** out_plan);
+/* Pathwise adjoint (no counterpart in the reference, which has no
+ * derivatives): a plan whose runs also return d E[payoffs[0]] / d params
+ * (grad_params, names of declared parameters) and / d X0 (grad_x0, process
+ * names), by a reverse sweep of Euler-Maruyama recomputed from checkpoints
+ * every opts->ckpt_every steps.  Euler only, no algebraic processes.  The
+ * run's estimates are [payoffs..., grad_params..., grad_x0...] per
+ * replicate (per-path sums and sums of squares).                          */
+int sde_plan_create_adjoint(const char* const* equations, int32_t n_equations,
+                            const char* const* param_names, int32_t n_params,
+                            const char* const* payoffs, int32_t n_payoffs,
+                            const char* const* grad_params, int32_t n_grad_params,
+                            const char* const* grad_x0, int32_t n_grad_x0,
+                            const sde_options* opts, sde_plan** out_plan);
+/* Number of estimator columns a run of this plan returns. */
+int sde_plan_n_estimates(const sde_plan* plan, int32_t* n);
 int sde_plan_destroy(sde_plan* plan);
 int sde_plan_n_processes(const sde_plan* plan, int32_t* n);
 int sde_plan_n_stochastic(const sde_plan* plan, int32_t* n);
@@ -169,7 +186,8 @@ int sde_result_copy_values(sde_result* r, double* host_out, int32_t layout);
 int sde_result_copy_long(sde_result* r, int32_t* scenario, double* time,
                          int32_t* process, double* value);
 /* Per replicate and estimator: sum and sum of squares of the payoff over
- * paths, FP64 with compensated summation; arrays [n_replicates][n_payoffs]. */
+ * paths, FP64 with compensated summation; arrays
+ * [n_replicates][sde_plan_n_estimates].                                   */
 int sde_result_estimates(sde_result* r, double* host_sum, double* host_sumsq);
 
 /* ---- known-answer kernels (device versions of the RNG building blocks) --

@@ -54,6 +54,8 @@ std::string emit(const ExprP& e, bool f32, const VarFn& var) {
         if (b->op == Op::Const && b->value == 0.5) return "sqrt(" + A(0) + ")";
         if (b->op == Op::Const && b->value == 2.0) return "sde_sq(" + A(0) + ")";
         if (b->op == Op::Const && b->value == 1.0) return A(0);
+        if (b->op == Op::Const && b->value == -0.5) return "sde_rsqrt(" + A(0) + ")";
+        if (b->op == Op::Const && b->value == -1.0) return "(" + lit(1.0, f32) + " / " + A(0) + ")";
         return "pow(" + A(0) + ", " + A(1) + ")";
     }
     case Op::Eq: return "sde_eq(" + A(0) + ", " + A(1) + ")";
@@ -104,6 +106,8 @@ std::string emit(const ExprP& e, bool f32, const VarFn& var) {
     case Fn::Sqrt: return fn1("sqrt");
     case Fn::Exp: return fn1("exp");
     case Fn::Step: return "sde_b(" + A(0) + " > " + lit(0.0, f32) + ", " + lit(0.0, f32) + ")";
+    case Fn::Mul0: return "sde_mul0(" + A(0) + ", " + A(1) + ")";
+    case Fn::Sel: return "(" + A(0) + " > " + lit(0.0, f32) + " ? " + A(1) + " : " + A(2) + ")";
     }
     return lit(NAN, f32);
 }
@@ -399,6 +403,156 @@ struct Gen {
         o.l("sde_block_reduce_store<" + S(K) + ">(f, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " + S(K) + "u) * 4u);");
     }
 
+    // ---- adjoint ---------------------------------------------------------
+    // Uniforms by random access (any step order): ChaCha blocks are cached
+    // per thread, Sobol points are direct.
+    void uniforms_ra(Out& o) const {
+        for (int k = 0; k < NI; ++k) {
+            const std::string K = S(k);
+            if (uses_chacha()) {
+                o.l("sde_u64 r" + K + ";");
+                o.l("{ const sde_u64 pos = (sde_u64)t * " + S(NI) + "ull + " + K + "ull;");
+                o.l("  if ((pos >> 3) != cblk) { cblk = pos >> 3; sde_chacha8_block(key, cblk, CB); }");
+                o.l("  const int w = (int)(pos & 7ull) * 2; r" + K + " = sde_pair(CB[w], CB[w + 1]); }");
+            }
+            if (sp.rng == RNG_PSEUDO) {
+                if (!f32) o.l("const double u" + K + " = sde_u64_to_f64(r" + K + ");");
+                else o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_u53(r" + K + " >> 11, q" + K + ", up" + K + ", gt" + K + ");");
+            } else if (sp.scramble == SCRAMBLE_SHIFT) {
+                o.l("const sde_u32 x" + K + " = sde_sobol_direct(a.sobol_v, t * " + S(NI) + " + " + K + ", G);");
+                if (!f32) {
+                    o.l("const double v" + K + " = (double)x" + K + " * 0x1p-32 + sde_u64_to_f64(r" + K + ");");
+                    o.l("const double u" + K + " = v" + K + " - trunc(v" + K + ");");
+                } else {
+                    o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_u53(sde_shift_u53(x" + K + ", r" + K + "), q" + K + ", up" + K + ", gt" + K + ");");
+                }
+            } else {
+                o.l("const int d" + K + " = t * " + S(NI) + " + " + K + ";");
+                o.l("if ((d" + K + " >> 5) != hchunk) { hchunk = d" + K + " >> 5; hval = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, hchunk, H, lane); }");
+                o.l("const sde_u32 y" + K + " = __shfl_sync(0xffffffffu, hval, d" + K + " & 31) ^ __ldg(&a.sobol_lo[(sde_u64)d" + K + " * 32u + L]);");
+                if (!f32) o.l("const double u" + K + " = ((double)y" + K + " + 0.5) * 0x1p-32;");
+                else o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_xor(y" + K + ", q" + K + ", up" + K + ", gt" + K + ");");
+            }
+        }
+    }
+
+    void step_header(Out& o) const {
+        o.l("const " + R + " tc = " + T("times") + ";");
+        o.l("const " + R + " tn = (" + R + ")__ldg(&a.times" + std::string(f32 ? "_f" : "") + "[t + 1]);");
+        o.l("const " + R + " dt = " + T("dts") + ";");
+        o.l("const " + R + " sdt = " + T("sqrt_dts") + ";");
+        o.l("(void)tc; (void)tn; (void)dt; (void)sdt;");
+    }
+
+    // increment k of a stochastic index as stored for the reverse sweep
+    std::string inc_store_name(int k) const {
+        return u.token_kind[k] == IncKind::Dw ? "w" + S(k) : "n" + S(k);
+    }
+
+    std::string adjoint(const std::string& name) const {
+        // Pathwise adjoint of Euler-Maruyama: X' = X + sum_j c_j(t, X, theta) inc_j,
+        // lambda_t = lambda_{t+1} + sum_p lambda_{t+1,p} sum_j dc_pj/dX inc_j,
+        // g_theta += sum_p lambda_{t+1,p} sum_j dc_pj/dtheta inc_j.  Increments
+        // are held fixed (common random numbers); jump counts are piecewise
+        // constant in the parameters.
+        const int E = sp.ckpt_every;
+        const int K = (int)sp.payoffs.size();
+        const int GP = (int)sp.grad_params.size(), GX = (int)sp.grad_x0.size();
+        Out o;
+        o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
+        o.ind++;
+        prologue(o);
+        if (uses_chacha()) o.l("sde_u64 cblk = ~0ull; sde_u32 CB[16];");
+        o.l(R + "* CK = (" + R + "*)a.ckpt;");
+        o.l("const sde_u64 ckrow = (sde_u64)rep * a.n_ckpt;");
+        // forward pass with checkpoints
+        o.l("for (int t = 0; t < n_steps; ++t) {");
+        o.ind++;
+        o.l("if (t % " + S(E) + " == 0 && active) {");
+        for (int p = 0; p < P; ++p)
+            o.l("  CK[((ckrow + t / " + S(E) + ") * " + S(P) + " + " + S(p) + ") * a.n_paths + i] = X" + S(p) + ";");
+        o.l("}");
+        step_header(o);
+        uniforms_ra(o);
+        wiener(o);
+        step_reference(o);
+        o.ind--;
+        o.l("}");
+        // payoffs and the terminal adjoint of payoff 0
+        o.l("const " + R + " tT = (" + R + ")__ldg(&a.times[a.T - 1]);");
+        o.l("double f[" + S(K + GP + GX) + "];");
+        for (int k = 0; k < K; ++k)
+            o.l("f[" + S(k) + "] = active ? (double)(" + ex(sp.payoffs[k], "X", "tT") + ") : 0.0;");
+        for (int p = 0; p < P; ++p)
+            o.l(R + " LA" + S(p) + " = " + ex(derivative(sp.payoffs[0], VarKind::Process, p), "X", "tT") + ";");
+        for (int m = 0; m < GP; ++m)
+            o.l(R + " GP" + S(m) + " = " + ex(derivative(sp.payoffs[0], VarKind::Param, sp.grad_params[m]), "X", "tT") + ";");
+        // reverse sweep over segments, recomputing each from its checkpoint
+        o.l(R + " LX[" + S(E * std::max(1, P)) + "];");
+        o.l(R + " LI[" + S(E * std::max(1, NI)) + "];");
+        o.l("const int nseg = (n_steps + " + S(E - 1) + ") / " + S(E) + ";");
+        o.l("for (int seg = nseg - 1; seg >= 0; --seg) {");
+        o.ind++;
+        o.l("const int s0 = seg * " + S(E) + ";");
+        o.l("const int s1 = min(s0 + " + S(E) + ", n_steps);");
+        for (int p = 0; p < P; ++p)
+            o.l("X" + S(p) + " = active ? CK[((ckrow + seg) * " + S(P) + " + " + S(p) + ") * a.n_paths + i] : X" + S(p) + ";");
+        o.l("for (int t = s0; t < s1; ++t) {");
+        o.ind++;
+        o.l("const int s = t - s0;");
+        for (int p = 0; p < P; ++p) o.l("LX[s * " + S(P) + " + " + S(p) + "] = X" + S(p) + ";");
+        step_header(o);
+        uniforms_ra(o);
+        wiener(o);
+        // record the stochastic increments (jump counts need the cache = X)
+        for (int p : u.levy) o.l("C" + S(p) + " = X" + S(p) + ";");
+        poisson(o, "C", "tc");
+        for (int k = 0; k < NI; ++k) o.l("LI[s * " + S(NI) + " + " + S(k) + "] = " + inc_store_name(k) + ";");
+        for (int p : u.levy) {
+            o.l(R + " N" + S(p) + " = X" + S(p) + ";");
+            for (const auto& tm : u.procs[p].terms)
+                o.l("N" + S(p) + " = N" + S(p) + " + " + ex(tm.coef, "C", "tc") + " * " + inc(tm) + ";");
+        }
+        for (int p : u.levy) o.l("X" + S(p) + " = N" + S(p) + ";");
+        o.ind--;
+        o.l("}");
+        o.l("for (int t = s1 - 1; t >= s0; --t) {");
+        o.ind++;
+        o.l("const int s = t - s0;");
+        o.l("const " + R + " tc = " + T("times") + ";");
+        o.l("const " + R + " dt = " + T("dts") + ";");
+        o.l("(void)tc; (void)dt;");
+        for (int p = 0; p < P; ++p) o.l("const " + R + " Y" + S(p) + " = LX[s * " + S(P) + " + " + S(p) + "];");
+        for (int k = 0; k < NI; ++k) o.l("const " + R + " " + inc_store_name(k) + " = LI[s * " + S(NI) + " + " + S(k) + "];");
+        for (int q = 0; q < P; ++q) o.l(R + " LN" + S(q) + " = " + L(0.0) + ";");
+        for (int p : u.levy) {
+            const auto& terms = u.procs[p].terms;
+            for (size_t j = 0; j < terms.size(); ++j) {
+                const ExprP& c = terms[j].coef;
+                const std::string li = "li" + S(p) + "_" + S((int)j);
+                o.l("{ const " + R + " " + li + " = LA" + S(p) + " * " + inc(terms[j]) + ";");
+                for (int q = 0; q < P; ++q)
+                    if (depends_on(c, VarKind::Process, q))
+                        o.l("  LN" + S(q) + " += " + li + " * " + ex(derivative(c, VarKind::Process, q), "Y", "tc") + ";");
+                for (int m = 0; m < GP; ++m)
+                    if (depends_on(c, VarKind::Param, sp.grad_params[m]))
+                        o.l("  GP" + S(m) + " += " + li + " * " + ex(derivative(c, VarKind::Param, sp.grad_params[m]), "Y", "tc") + ";");
+                o.l("}");
+            }
+        }
+        for (int q = 0; q < P; ++q) o.l("LA" + S(q) + " += LN" + S(q) + ";");
+        o.ind--;
+        o.l("}");
+        o.ind--;
+        o.l("}");
+        for (int m = 0; m < GP; ++m) o.l("f[" + S(K + m) + "] = active ? (double)GP" + S(m) + " : 0.0;");
+        for (int x = 0; x < GX; ++x) o.l("f[" + S(K + GP + x) + "] = active ? (double)LA" + S(sp.grad_x0[x]) + " : 0.0;");
+        o.l("sde_block_reduce_store<" + S(K + GP + GX) + ">(f, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " + S(K + GP + GX) + "u) * 4u);");
+        o.ind--;
+        o.l("}");
+        return o.s.str();
+    }
+
     std::string forward(const std::string& name) const {
         Out o;
         o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
@@ -437,6 +591,7 @@ std::string generate_source(const Universe& u, const KernelSpec& s) {
     Gen g(u, s);
     std::string src;
     src += g.forward(forward_kernel_name(s));
+    if (s.adjoint) src += "\n" + g.adjoint(adjoint_kernel_name(s));
     return src;
 }
 

