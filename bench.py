@@ -51,6 +51,36 @@ def times():
     return [i / STEPS_T for i in range(STEPS_T + 1)]
 
 
+# ---- 64-dimensional correlated basket --------------------------------------
+
+def basket_equations(dim: int = 64, seed: int = 2024):
+    """GBM basket in the reference grammar: sigma_i ~ U(0.1, 0.5), mu = 0.02,
+    correlation 0.3 off the diagonal plus a 0.2-scaled random-orthogonal
+    perturbation, projected to PSD (eigenvalues clipped, unit diagonal
+    restored), FP64 Cholesky factor L.  Process i's diffusion terms are
+    (L_ij sigma_i * S_i) * dW_j, j <= i."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sigma = rng.uniform(0.1, 0.5, dim)
+    q, _ = np.linalg.qr(rng.standard_normal((dim, dim)))
+    pert = q @ np.diag(rng.uniform(-1.0, 1.0, dim)) @ q.T
+    np.fill_diagonal(pert, 0.0)
+    corr = 0.3 * (np.ones((dim, dim)) - np.eye(dim)) + np.eye(dim) + 0.2 * pert
+    w, v = np.linalg.eigh((corr + corr.T) / 2)
+    corr = v @ np.diag(np.clip(w, 1e-6, None)) @ v.T
+    d = np.sqrt(np.diag(corr))
+    corr = corr / np.outer(d, d)
+    L = np.linalg.cholesky(corr)
+    eqs = []
+    for i in range(dim):
+        terms = [f"(0.02 * S{i + 1}) * dt"]
+        for j in range(i + 1):
+            terms.append(f"({float(L[i, j] * sigma[i])!r} * S{i + 1}) * dW{j + 1}")
+        eqs.append(f"dS{i + 1} = " + " + ".join(terms))
+    payoff = "max((" + " + ".join(f"S{i + 1}" for i in range(dim)) + f") / {dim} - 100, 0)"
+    return eqs, payoff, sigma, L
+
+
 def dist_init(n_gpus):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -280,6 +310,267 @@ def run_engine(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# Other configurations (not the default line): the reference's plain GBM,
+# the batched instances, the pathwise adjoint and the 64-dim basket.
+# ---------------------------------------------------------------------------
+
+GBM = ["dX = (0.05 * X) * dt + (0.2 * X) * dW1"]
+GBM_P = ["dX = (mu * X) * dt + (sigma * X) * dW1"]
+OU_P = ["dX = (theta * (m - X)) * dt + (s) * dW1"]
+HESTON_P = ["dv = (kappa * (theta - max(v, 0))) * dt + (xi * max(v, 0)^0.5) * dW1",
+            "dS = (mu * S) * dt + (rho * max(v, 0)^0.5 * S) * dW1 + "
+            "((1 - rho^2)^0.5 * max(v, 0)^0.5 * S) * dW2"]
+
+
+def batched_instances(n=4096, seed=11, max_steps=1024, max_log2_paths=16):
+    """Half GBM (mu ~ U(-0.05, 0.10), sigma ~ U(0.05, 0.6), X0 ~ U(50, 150)),
+    half OU (theta ~ U(0.5, 5), m ~ N(0, 1), s ~ U(0.1, 1), X0 ~ N(0, 1));
+    steps ~ U{16..max_steps}, paths = floor(2^U(8, max_log2_paths)), T = 1."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    half = n // 2
+    tid = np.array([0] * half + [1] * (n - half), dtype=np.int32)
+    steps = rng.integers(16, max_steps + 1, size=n)
+    paths = np.floor(2.0 ** rng.uniform(8, max_log2_paths, size=n)).astype(np.uint64)
+    params = np.zeros((n, 3))
+    x0 = np.zeros((n, 1))
+    params[:half, 0] = rng.uniform(-0.05, 0.10, half)
+    params[:half, 1] = rng.uniform(0.05, 0.6, half)
+    x0[:half, 0] = rng.uniform(50, 150, half)
+    params[half:, 0] = rng.uniform(0.5, 5, n - half)
+    params[half:, 1] = rng.normal(0, 1, n - half)
+    params[half:, 2] = rng.uniform(0.1, 1, n - half)
+    x0[half:, 0] = rng.normal(0, 1, n - half)
+    seeds = np.arange(n, dtype=np.uint64) * np.uint64(1 << 20) + np.uint64(seed)
+    return tid, steps, paths, seeds, x0, params
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def _timed_runs(fn, steps, stream, flush):
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    out = []
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        ev[k][0].record(stream)
+        out.append(fn())
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev], out
+
+
+def _common(args, workload, metric, value, ms, dtype, clocks, e2e, launches, roofline, cpu, extra):
+    line = {"metric": metric, "value": value, "unit": "path-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": dict(workload=workload, l2="flushed (256 MiB write) between timed steps", **extra),
+            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
+def run_gbm_full(args):
+    """The reference's plain configuration: GBM, Euler, 252 steps, 10,000
+    paths, ChaCha8 seed 42, FP64, full filtration of 253 time points."""
+    import numpy as np
+    import torch
+    import sde_sim_rs
+    from oracle import oracle as O
+    n, T = 10000, [i / 252 for i in range(253)]
+    plan = sde_sim_rs.Plan(GBM, precision="fp64", output="full")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    one = lambda: plan.run(T, {"X": 100.0}, n, seed=42, stream=stream)
+    for _ in range(args.warmup):
+        one().wait()
+    with Clocks(0) as clk:
+        ms, res = _timed_runs(one, args.steps, stream, flush)
+    ms_step = sum(ms) / len(ms)
+    ps = n * 252
+    xt = res[-1].values("device")[0, -1, 0]
+    t0 = time.perf_counter()
+    for _ in range(3):
+        fr = sde_sim_rs.simulate(GBM, T, n, {"X": 100.0}, "pseudo", "euler", seed=42, output_format="numpy")
+    e2e_s = (time.perf_counter() - t0) / 3
+    rows = len(fr["value"])
+    nbytes = n * 253 * 8
+    peak = _peaks()
+    u = O.Universe(GBM)
+    c0 = time.perf_counter()
+    u.simulate(T, {"X": 100.0}, 0, n, seed=42, threads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - c0
+    _common(args, "gbm_euler_fp64_10000x253_full", "path-steps/s (fwd, GBM full filtration, FP64)",
+            ps / (ms_step * 1e-3), ms_step, "f64", clk.summary(),
+            {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 253 * 28,
+             "d2h_bytes_per_step": rows * (4 + 8 + 4 + 8), "through": "sde_sim_rs.simulate (long frame)"},
+            2 * args.steps,
+            {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
+             "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"], "traffic": None,
+             "note": "10,000 paths fill 40 blocks: latency-bound, not a bandwidth case"},
+            {"value": ps / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
+             "sample": "full size (10,000 paths x 252 steps, full filtration)"},
+            {"paths": n, "steps": 252, "mean_XT": float(xt.mean()), "exact_mean": 100 * math.exp(0.05),
+             "std_XT": float(xt.std()), "exact_std": 100 * math.exp(0.05) * math.sqrt(math.exp(0.04) - 1)})
+
+
+def run_basket(args):
+    """64-dim correlated GBM basket: Euler, 128 steps, 2^21 paths, XOR Sobol
+    dimension 8192, FP32 filtration at 32 equally spaced checkpoints."""
+    import numpy as np
+    import torch
+    import sde_sim_rs
+    from oracle import oracle as O
+    eqs, payoff, _, _ = basket_equations()
+    n = args.paths if args.paths != N_PATHS else 1 << 21
+    T = [i / 128 for i in range(129)]
+    ck = list(range(4, 129, 4))
+    plan = sde_sim_rs.Plan(eqs, payoffs=[payoff], rng="sobol", scramble="xor", precision="fp32",
+                           output="checkpoints")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    one = lambda: plan.run(T, {f"S{i + 1}": 100.0 for i in range(64)}, n, seed=7, checkpoints=ck, stream=stream)
+    for _ in range(args.warmup):
+        one().wait()
+    with Clocks(0) as clk:
+        ms, res = _timed_runs(one, args.steps, stream, flush)
+    ms_step = sum(ms) / len(ms)
+    s, q = res[-1].estimates()
+    price = s[0, 0] / n
+    se = math.sqrt(max(q[0, 0] / n - price ** 2, 0) / n)
+    del res
+    ps = n * 128
+    nbytes = n * 64 * 32 * 4
+    peak = _peaks()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        one().estimates()
+    e2e_s = (time.perf_counter() - t0) / 2
+    u = O.Universe(eqs)
+    cpu_n = 512
+    c0 = time.perf_counter()
+    u.estimate(T, {f"S{i + 1}": 100.0 for i in range(64)}, 0, cpu_n, payoff, rng=O.SOBOL, scramble=O.XOR,
+               seed=7, n_per_replicate=n, threads=os.cpu_count() or 1)
+    cpu_s = time.perf_counter() - c0
+    _common(args, "basket64_euler_fp32_sobolxor_2^21x128_32ckpt", "path-steps/s (fwd, 64-dim basket, FP32)",
+            ps / (ms_step * 1e-3), ms_step, "f32", clk.summary(),
+            {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 129 * 28 + 64 * 8,
+             "d2h_bytes_per_step": 16, "note": "filtration stays in HBM; the estimate is read back"},
+            3 * args.steps,
+            {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
+             "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"], "traffic": None,
+             "bytes_written_per_launch": nbytes},
+            {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
+             "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, estimator only"},
+            {"paths": n, "steps": 128, "checkpoints": 32, "price": price, "price_se": se})
+
+
+def run_batched(args):
+    """4096 uneven GBM / OU instances in one persistent graph-captured launch
+    (FP32), against 4096 plain per-instance FP64 launches."""
+    import numpy as np
+    import torch
+    import sde_sim_rs
+    from sde_sim_rs.batch import Batch
+    tid, steps, paths, seeds, x0, params = batched_instances()
+    tg = sde_sim_rs.Plan(GBM_P, params=["mu", "sigma"], payoffs=["X"], precision="fp32", output="none")
+    to = sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], precision="fp32", output="none")
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    t0 = time.perf_counter()
+    job = Batch([tg, to]).prepare(tid, steps, 1.0, paths, seeds, x0, params, autotune=True, stream=stream)
+    prep_s = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        job.run(stream).results()
+    with Clocks(0) as clk:
+        ms, _ = _timed_runs(lambda: job.run(stream), args.steps, stream, flush)
+    ms_step = sum(ms) / len(ms)
+    ps = job.path_steps
+    s, q = job.results()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        job.run(stream).results()
+    e2e_s = (time.perf_counter() - t0) / 3
+    # baseline: plain per-instance FP64 launches
+    pg = sde_sim_rs.Plan(GBM_P, params=["mu", "sigma"], payoffs=["X"], precision="fp64", output="none")
+    po = sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], precision="fp64", output="none")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = []
+    for i in range(len(tid)):
+        plan = pg if tid[i] == 0 else po
+        res.append(plan.run(np.arange(steps[i] + 1) / steps[i], {"X": x0[i, 0]}, int(paths[i]), seed=int(seeds[i]),
+                            params=params[i, :len(plan.params)], stream=stream))
+    torch.cuda.synchronize()
+    fp64_s = time.perf_counter() - t0
+    z = []
+    for i, r in enumerate(res):
+        rs, rq = r.estimates()
+        N = float(paths[i])
+        m64 = rs[0, 0] / N
+        se = math.sqrt(max(rq[0, 0] / N - m64 ** 2, 0) / N)
+        z.append(abs(s[i, 0] / N - m64) / max(se, 1e-300))
+    z = np.array(z)
+    _common(args, "batched_4096_gbm_ou_fp32", "path-steps/s (fwd, 4096 batched instances, FP32)",
+            ps / (ms_step * 1e-3), ms_step, "f32", clk.summary(),
+            {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
+             "d2h_bytes_per_step": len(tid) * 16, "note": "graph replay + results read back"},
+            2 * args.steps, None, None,
+            {"instances": len(tid), "path_steps": ps, "block": job.block, "paths_per_thread": job.paths_per_thread,
+             "work_items": job.n_items, "prepare_s": prep_s,
+             "fp64_per_instance_launches": {"value": ps / fp64_s, "unit": "path-steps/s", "seconds": fp64_s},
+             "speedup_vs_fp64_launches": (ps / (ms_step * 1e-3)) / (ps / fp64_s),
+             "fraction_within_3se_of_fp64": float(np.mean(z < 3)), "max_z": float(z.max())})
+
+
+def run_adjoint(args):
+    """Pathwise adjoint Greeks, 2^20 paths, 365 steps, FP32 forward + reverse,
+    checkpoints every 19 steps, against the plain FP64 GPU forward pass."""
+    import numpy as np
+    import torch
+    import sde_sim_rs
+    n, T = 1 << 20, np.linspace(0.0, 1.0, 366)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, eqs, params, gp, gx, init, pay in (
+            ("gbm", GBM_P, {"mu": 0.05, "sigma": 0.2}, ["mu", "sigma"], ["X"], {"X": 100.0}, "max(X - 100, 0)"),
+            ("heston", HESTON_P, {"kappa": 2.0, "theta": 0.04, "xi": 0.3, "rho": -0.7, "mu": 0.03},
+             ["kappa", "theta", "xi", "rho"], ["v"], {"S": 100.0, "v": 0.04}, "max(S - 100, 0)")):
+        adj = sde_sim_rs.Plan(eqs, params=list(params), payoffs=[pay], grad_params=gp, grad_x0=gx,
+                              precision="fp32", output="none")
+        f64 = sde_sim_rs.Plan(eqs, params=list(params), payoffs=[pay], precision="fp64", output="none")
+        one_a = lambda: adj.run(T, init, n, seed=42, params=params, stream=stream)
+        one_f = lambda: f64.run(T, init, n, seed=42, params=params, stream=stream)
+        for _ in range(args.warmup):
+            one_a().wait()
+        one_f().wait()
+        ms_a, ra = _timed_runs(one_a, args.steps, stream, flush)
+        ms_f, rf = _timed_runs(one_f, 2, stream, flush)
+        s, q = ra[-1].estimates()
+        m = s[0] / n
+        se = np.sqrt(np.maximum(q[0] / n - m * m, 0) / n)
+        s64, q64 = rf[-1].estimates()
+        ta, tf = sum(ms_a) / len(ms_a), sum(ms_f) / len(ms_f)
+        out[name] = {"fwd_adjoint_path_steps_per_s": n * 365 / (ta * 1e-3),
+                     "fp64_fwd_path_steps_per_s": n * 365 / (tf * 1e-3),
+                     "speedup_fp32_fwd_adj_vs_fp64_fwd": tf / ta,
+                     "price_fp32": float(m[0]), "price_fp64": float(s64[0, 0] / n), "price_se": float(se[0]),
+                     "gradients": dict(zip(gp + gx, [float(x) for x in m[1:]])),
+                     "gradient_se": dict(zip(gp + gx, [float(x) for x in se[1:]])), "ms": ta}
+    g = out["gbm"]
+    _common(args, "adjoint_gbm_heston_2^20x365", "path-steps/s (fwd+adjoint, GBM, FP32)",
+            g["fwd_adjoint_path_steps_per_s"], g["ms"], "f32", None, None, 2 * args.steps, None, None, out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -291,13 +582,20 @@ def main():
     ap.add_argument("--reps", type=int, default=REPS)
     ap.add_argument("--fp64-paths", type=int, default=1 << 14)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--workload", default="heston_rqmc",
+                    choices=["heston_rqmc", "gbm_full", "basket", "batched", "adjoint"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.workload == "heston_rqmc":
         run_engine(args)
+    else:
+        import torch
+        torch.cuda.set_device(0)
+        {"gbm_full": run_gbm_full, "basket": run_basket, "batched": run_batched,
+         "adjoint": run_adjoint}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -76,7 +76,9 @@ typedef struct sde_options {
     int32_t block_size;     /* threads per block, 0 = 256                  */
     int32_t ckpt_every;     /* adjoint plans: steps between checkpoints,
                                0 = 19                                      */
-    int32_t reserved[7];
+    int32_t paths_per_thread; /* independent paths a thread steps in
+                               lockstep (1, 2 or 4), 0 = 1                 */
+    int32_t reserved[6];
 } sde_options;
 
 typedef struct sde_run_args {
@@ -147,6 +149,8 @@ int sde_plan_process_index(const sde_plan* plan, const char* name, int32_t* inde
 int sde_plan_stochastic_token(const sde_plan* plan, int32_t i, char* buf, size_t buf_len);
 /* The generated CUDA C (for inspection); *needed gets the size incl. NUL. */
 int sde_plan_source(const sde_plan* plan, char* buf, size_t buf_len, size_t* needed);
+/* The NVRTC / ptxas log of the plan's compilation (registers, spills). */
+int sde_plan_compile_log(const sde_plan* plan, char* buf, size_t buf_len, size_t* needed);
 
 /* ---- runs --------------------------------------------------------------
  * Replaces the scenario loop of sde_sim_rs::sim::simulate
@@ -189,6 +193,46 @@ int sde_result_copy_long(sde_result* r, int32_t* scenario, double* time,
  * paths, FP64 with compensated summation; arrays
  * [n_replicates][sde_plan_n_estimates].                                   */
 int sde_result_estimates(sde_result* r, double* host_sum, double* host_sumsq);
+
+/* ---- batched instances ---------------------------------------------------
+ * No counterpart in the reference (one universe per simulate call): many
+ * independent instances of a few templates (plans from sde_plan_create,
+ * pseudo-random, same precision), each with its own uniform step count,
+ * horizon, path count, seed, initial values and parameters, run by one
+ * persistent work-queue kernel captured in a CUDA graph.  Paths per thread
+ * and block shape come from a timing autotuner at prepare time.           */
+typedef struct sde_batch sde_batch;
+typedef struct sde_batch_job sde_batch_job;
+
+typedef struct sde_batch_instances {
+    uint32_t struct_size;       /* sizeof(sde_batch_instances)                 */
+    int32_t n_instances;
+    const int32_t* template_id; /* host [n]: index into the batch's templates  */
+    const int32_t* n_steps;     /* host [n]: uniform steps on [0, t_end]       */
+    const double* t_end;        /* host [n]                                    */
+    const uint64_t* n_paths;    /* host [n]                                    */
+    const uint64_t* seed;       /* host [n]: path s uses seed_from_u64(seed+s) */
+    const double* x0;           /* host [n][x0_stride] by process index        */
+    int32_t x0_stride;
+    const double* params;       /* host [n][param_stride] by parameter index   */
+    int32_t param_stride;
+} sde_batch_instances;
+
+int sde_batch_create(const sde_plan* const* templates, int32_t n_templates, sde_batch** out_batch);
+int sde_batch_destroy(sde_batch* batch);
+/* Uploads the instances, builds the work queue (longest instances first),
+ * picks (block, paths per thread) by timing each candidate when autotune is
+ * nonzero, and captures the launch in a CUDA graph.                      */
+int sde_batch_prepare(sde_batch* batch, const sde_batch_instances* inst, int32_t autotune,
+                      void* stream, sde_batch_job** out_job);
+/* Replays the graph: one persistent launch over every instance. */
+int sde_batch_job_run(sde_batch_job* job, void* stream);
+/* Waits; per instance and payoff: sum and sum of squares over its paths,
+ * arrays [n_instances][n_payoffs] (n_payoffs = the largest template's).  */
+int sde_batch_job_results(sde_batch_job* job, double* host_sum, double* host_sumsq);
+int sde_batch_job_info(const sde_batch_job* job, int32_t* block, int32_t* paths_per_thread,
+                       int32_t* n_items, uint64_t* path_steps, int32_t* n_payoffs);
+int sde_batch_job_destroy(sde_batch_job* job);
 
 /* ---- known-answer kernels (device versions of the RNG building blocks) --
  * rand_chacha ChaCha8Rng::seed_from_u64(seed), u64 values [first, first+n)

@@ -1,14 +1,22 @@
-// codegen.cpp -- lowers a process universe to one CUDA kernel per plan.
+// codegen.cpp -- lowers a process universe to CUDA kernels.
 //
-// One thread owns one path for the whole time loop (src/sim/mod.rs:41-87 is
-// the reference's loop over scenarios and steps).  Every coefficient is an
-// inline expression, so the step loop interprets nothing.  The step body
-// follows euler_iteration (src/sim/euler.rs:5-37) or runge_kutta_iteration
-// (src/sim/runge_kutta.rs:5-107) including the reference's name->value cache
-// (src/func.rs:32-42, src/filtration.rs:70-79), which the lowered code keeps
-// in registers C<p> and refreshes exactly where the reference refreshes it.
+// A thread owns PPT paths (lanes j = 0..PPT-1) for the whole time loop
+// (src/sim/mod.rs:41-87 is the reference's loop over scenarios and steps).
+// Every coefficient is an inline expression, so the step loop interprets
+// nothing.  The step body follows euler_iteration (src/sim/euler.rs:5-37) or
+// runge_kutta_iteration (src/sim/runge_kutta.rs:5-107), including the
+// reference's name->value cache (src/func.rs:32-42, src/filtration.rs:70-79),
+// which the lowered code keeps in registers C<p> and refreshes exactly where
+// the reference refreshes it.
+//
+// Three kernels come out of the same emitters:
+//   forward  -- one plan, grid over (paths / (block*PPT), replicates)
+//   adjoint  -- forward with checkpoints, then a pathwise reverse sweep
+//   batch    -- per-template device functions called from a persistent
+//               work-queue kernel over many instances
 #include "codegen.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <functional>
@@ -49,7 +57,7 @@ std::string emit(const ExprP& e, bool f32, const VarFn& var) {
     case Op::Mod: return "fmod(" + A(0) + ", " + A(1) + ")";
     case Op::Pow: {
         // x^0.5 is lowered to sqrt (equal to a correctly rounded pow for
-        // every x >= 0), x^2 to x*x and x^1 to x.
+        // every x >= 0), x^2 to x*x, x^1 to x, x^-0.5 to rsqrt, x^-1 to 1/x.
         const ExprP& b = e->args[1];
         if (b->op == Op::Const && b->value == 0.5) return "sqrt(" + A(0) + ")";
         if (b->op == Op::Const && b->value == 2.0) return "sde_sq(" + A(0) + ")";
@@ -123,94 +131,147 @@ struct Out {
 
 std::string S(int v) { return std::to_string(v); }
 
-// Shared emitter state for one kernel.
+enum class Mode { Forward, Batch };
+
 struct Gen {
     const Universe& u;
     const KernelSpec& sp;
     bool f32;
     std::string R;
     int P, NI;
+    Mode mode = Mode::Forward;
+    int ppt = 1;
+    std::string sfx;  // per-lane suffix of per-path names
 
     Gen(const Universe& uu, const KernelSpec& s)
         : u(uu), sp(s), f32(s.precision == PREC_FP32), R(f32 ? "float" : "double"),
-          P(uu.n_processes()), NI(uu.n_stochastic()) {}
+          P(uu.n_processes()), NI(uu.n_stochastic()), ppt(std::max(1, s.ppt)) {}
 
     std::string L(double v) const { return lit(v, f32); }
-    std::string T(const char* arr) const { return std::string("__ldg(&a.") + arr + (f32 ? "_f" : "") + "[t])"; }
+    // per-path (per-lane) names
+    std::string V(const std::string& b, int i) const { return b + S(i) + sfx; }
+    std::string V(const std::string& b) const { return b + sfx; }
+    void lane(int j) { sfx = ppt > 1 ? "_" + S(j) : ""; }
 
-    // Expression with processes read from the named register set and time
-    // from the named variable.
+    std::string T(const char* arr, const char* idx = "t") const {
+        return std::string("__ldg(&a.") + arr + (f32 ? "_f" : "") + "[" + idx + "])";
+    }
+
+    // Expression with processes read from the named per-lane register set.
     std::string ex(const ExprP& e, const std::string& procset, const std::string& tvar) const {
         return emit(e, f32, [&](VarKind k, int i) -> std::string {
-            if (k == VarKind::Process) return procset + S(i);
-            if (k == VarKind::Time) return tvar;
-            if (k == VarKind::Param) return "PR" + S(i);
-            return "0";
-        });
-    }
-    // Expression with a per-process name function
-    std::string exf(const ExprP& e, const std::function<std::string(int)>& proc, const std::string& tvar) const {
-        return emit(e, f32, [&](VarKind k, int i) -> std::string {
-            if (k == VarKind::Process) return proc(i);
+            if (k == VarKind::Process) return V(procset, i);
             if (k == VarKind::Time) return tvar;
             if (k == VarKind::Param) return "PR" + S(i);
             return "0";
         });
     }
 
+    bool xorm() const { return sp.rng == RNG_SOBOL && sp.scramble == SCRAMBLE_XOR; }
+    bool shiftm() const { return sp.rng == RNG_SOBOL && sp.scramble == SCRAMBLE_SHIFT; }
+    // Steps per unrolled group: whole ChaCha blocks (8 u64) for the pseudo /
+    // shift streams, whole 32-dimension Sobol chunks for the XOR mode, so
+    // every block word and every shuffle lane is a compile-time constant.
     int group() const {
         if (NI == 0) return 1;
-        if (sp.rng == RNG_SOBOL && sp.scramble == SCRAMBLE_XOR) return 1;
+        if (xorm()) return 32 / std::gcd(NI, 32);
         return 8 / std::gcd(NI, 8);
     }
-    bool uses_chacha() const { return NI > 0 && !(sp.rng == RNG_SOBOL && sp.scramble == SCRAMBLE_XOR); }
+    // the FP32 XOR path goes straight from the scrambled word to a normal;
+    // q / up / gt are formed only where a jump count or RK's sign needs them
+    bool needs_tail(int k) const {
+        return u.token_kind[k] == IncKind::Dn || (sp.scheme == SCHEME_RK && k == 0);
+    }
+    bool uses_chacha() const { return NI > 0 && !xorm(); }
     bool has_alg() const { return !u.alg.empty(); }
 
-    // ---- uniforms of step t -------------------------------------------
+    // ---- uniforms of step t for the current lane ------------------------
+    // Forward / batch kernels: step groups of U steps hold whole ChaCha
+    // blocks in registers (indices known at compile time).
+    void uniform_from(Out& o, int k) const {
+        const std::string K = S(k);
+        if (sp.rng == RNG_PSEUDO) {
+            if (!f32) o.l("const double " + V("u", k) + " = sde_u64_to_f64(" + V("r", k) + ");");
+            else o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_u53(" +
+                     V("r", k) + " >> 11, " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
+        } else if (shiftm()) {
+            o.l("const sde_u32 " + V("x", k) + " = sde_sobol_direct(a.sobol_v, t * " + S(NI) + " + " + K + ", " + V("G") + ");");
+            if (!f32) {
+                o.l("const double " + V("v", k) + " = (double)" + V("x", k) + " * 0x1p-32 + sde_u64_to_f64(" + V("r", k) + ");");
+                o.l("const double " + V("u", k) + " = " + V("v", k) + " - trunc(" + V("v", k) + ");");
+            } else {
+                o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_u53(sde_shift_u53(" +
+                    V("x", k) + ", " + V("r", k) + "), " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
+            }
+        } else {
+            o.l("const int " + V("d", k) + " = t * " + S(NI) + " + " + K + ";");
+            o.l("if ((" + V("d", k) + " >> 5) != " + V("hchunk") + ") { " + V("hchunk") + " = " + V("d", k) +
+                " >> 5; " + V("hval") + " = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, " + V("hchunk") +
+                ", " + V("H") + ", lane); }");
+            o.l("const sde_u32 " + V("y", k) + " = __shfl_sync(0xffffffffu, " + V("hval") + ", " + V("d", k) +
+                " & 31) ^ __ldg(&a.sobol_lo[(sde_u64)" + V("d", k) + " * 32u + " + V("L") + "]);");
+            if (!f32) o.l("const double " + V("u", k) + " = ((double)" + V("y", k) + " + 0.5) * 0x1p-32;");
+            else o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_xor(" + V("y", k) +
+                     ", " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
+        }
+    }
+
     void uniforms(Out& o, int g, std::vector<bool>& block_done) const {
         for (int k = 0; k < NI; ++k) {
-            const std::string K = S(k);
+            if (xorm()) {
+                // dimension t*NI + k = group base (a multiple of 32) + e
+                const int e = g * NI + k, c = e / 32, l = e % 32;
+                if (!block_done[c]) {
+                    o.l(V("hv", c) + " = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, chunk0 + " + S(c) + ", " +
+                        V("H") + ", lane);");
+                    block_done[c] = true;
+                }
+                o.l("const sde_u32 " + V("y", k) + " = __shfl_sync(0xffffffffu, " + V("hv", c) + ", " + S(l) +
+                    ") ^ __ldg(" + V("LOp") + " + " + S(e * 32) + ");");
+                if (!f32) o.l("const double " + V("u", k) + " = ((double)" + V("y", k) + " + 0.5) * 0x1p-32;");
+                else if (needs_tail(k))
+                    o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_xor(" +
+                        V("y", k) + ", " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
+                continue;
+            }
             if (uses_chacha()) {
                 int pos = g * NI + k, b = pos / 8, w = (pos % 8) * 2;
                 if (!block_done[b]) {
-                    o.l("sde_chacha8_block(key, blk0 + " + S(b) + "ull, B" + S(b) + ");");
+                    o.l("sde_chacha8_block(" + V("key") + ", blk0 + " + S(b) + "ull, " + V("B", b) + ");");
                     block_done[b] = true;
                 }
-                o.l("const sde_u64 r" + K + " = sde_pair(B" + S(b) + "[" + S(w) + "], B" + S(b) + "[" + S(w + 1) + "]);");
+                o.l("const sde_u64 " + V("r", k) + " = sde_pair(" + V("B", b) + "[" + S(w) + "], " + V("B", b) + "[" +
+                    S(w + 1) + "]);");
             }
-            if (sp.rng == RNG_PSEUDO) {
-                if (!f32) o.l("const double u" + K + " = sde_u64_to_f64(r" + K + ");");
-                else o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_u53(r" + K + " >> 11, q" + K + ", up" + K + ", gt" + K + ");");
-            } else if (sp.scramble == SCRAMBLE_SHIFT) {
-                o.l("const sde_u32 x" + K + " = sde_sobol_direct(a.sobol_v, t * " + S(NI) + " + " + K + ", G);");
-                if (!f32) {
-                    o.l("const double v" + K + " = (double)x" + K + " * 0x1p-32 + sde_u64_to_f64(r" + K + ");");
-                    o.l("const double u" + K + " = v" + K + " - trunc(v" + K + ");");
-                } else {
-                    o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_u53(sde_shift_u53(x" + K + ", r" + K + "), q" + K + ", up" + K + ", gt" + K + ");");
-                }
-            } else {
-                o.l("const int d" + K + " = t * " + S(NI) + " + " + K + ";");
-                o.l("if ((d" + K + " >> 5) != hchunk) { hchunk = d" + K + " >> 5; hval = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, hchunk, H, lane); }");
-                o.l("const sde_u32 y" + K + " = __shfl_sync(0xffffffffu, hval, d" + K + " & 31) ^ __ldg(&a.sobol_lo[(sde_u64)d" + K + " * 32u + L]);");
-                if (!f32) o.l("const double u" + K + " = ((double)y" + K + " + 0.5) * 0x1p-32;");
-                else o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_xor(y" + K + ", q" + K + ", up" + K + ", gt" + K + ");");
+            uniform_from(o, k);
+        }
+    }
+
+    // Random access by step (adjoint): ChaCha blocks cached per thread.
+    void uniforms_ra(Out& o) const {
+        for (int k = 0; k < NI; ++k) {
+            if (uses_chacha()) {
+                o.l("sde_u64 " + V("r", k) + ";");
+                o.l("{ const sde_u64 pos = (sde_u64)t * " + S(NI) + "ull + " + S(k) + "ull;");
+                o.l("  if ((pos >> 3) != cblk) { cblk = pos >> 3; sde_chacha8_block(" + V("key") + ", cblk, CB); }");
+                o.l("  const int w = (int)(pos & 7ull) * 2; " + V("r", k) + " = sde_pair(CB[w], CB[w + 1]); }");
             }
+            uniform_from(o, k);
         }
     }
 
     // Wiener increments w<k> = sqrt_dt * icdf(u<k>)   (increment.rs:89-97)
-    void wiener(Out& o) const {
+    void wiener(Out& o, bool from_words = false) const {
         for (int k = 0; k < NI; ++k) {
             if (u.token_kind[k] != IncKind::Dw) continue;
-            const std::string K = S(k);
-            if (!f32) o.l("const double w" + K + " = sdt * sde_icdf_as26(u" + K + ");");
-            else o.l("const float w" + K + " = sdt * sde_icdf_as26_q(q" + K + ", up" + K + ");");
+            if (!f32) o.l("const double " + V("w", k) + " = sdt * sde_icdf_as26(" + V("u", k) + ");");
+            else if (from_words) o.l("const float " + V("w", k) + " = sdt * sde_normal_xor(" + V("y", k) + ");");
+            else o.l("const float " + V("w", k) + " = sdt * sde_icdf_as26_q(" + V("q", k) + ", " + V("up", k) + ");");
         }
     }
 
-    // Poisson increments n<k> (increment.rs:137-148); lambda read through
-    // the given register set at time tvar.
+    // Poisson increments n<k> (increment.rs:137-148); the intensity is read
+    // through the given register set at time tvar.
     void poisson(Out& o, const std::string& procset, const std::string& tvar) const {
         for (int k = 0; k < NI; ++k) {
             if (u.token_kind[k] != IncKind::Dn) continue;
@@ -218,250 +279,381 @@ struct Gen {
             for (const auto& p : u.procs)
                 for (const auto& t : p.terms)
                     if (t.sidx == k && t.lambda) lam = t.lambda;
-            const std::string K = S(k);
-            std::string pu = f32 ? "(up" + K + " ? 1.0f - q" + K + " : q" + K + ")" : "u" + K;
-            o.l("const " + R + " n" + K + " = sde_poisson(" + pu + ", " + ex(lam, procset, tvar) + " * dt);");
+            std::string pu = f32 ? "(" + V("up", k) + " ? 1.0f - " + V("q", k) + " : " + V("q", k) + ")" : V("u", k);
+            o.l("const " + R + " " + V("n", k) + " = sde_poisson(" + pu + ", " + ex(lam, "C", tvar) + " * dt);");
+            (void)procset;
         }
     }
 
     std::string inc(const Term& t) const {
         if (t.kind == IncKind::Dt) return "dt";
-        if (t.kind == IncKind::Dw) return "w" + S(t.sidx);
-        return "n" + S(t.sidx);
+        if (t.kind == IncKind::Dw) return V("w", t.sidx);
+        return V("n", t.sidx);
     }
 
     std::string sk_expr() const {
-        if (!f32) return "(u0 > 0.5 ? 1.0 : -1.0)";
-        return "(gt0 ? 1.0f : -1.0f)";
+        // with no stochastic index the reference panics at the first step
+        // (src/rng/pseudo.rs:53-57); runs with steps are refused on the host
+        if (NI == 0) return L(1.0);
+        if (!f32) return "(" + V("u", 0) + " > 0.5 ? 1.0 : -1.0)";
+        return "(" + V("gt", 0) + " ? 1.0f : -1.0f)";
     }
 
-    // ---- one step, reference semantics --------------------------------
+    // coefficient k * X_q (or X_q * k) -> (k, q); k may be any expression:
+    // sum_j (k_j X_q) inc_j = X_q sum_j k_j inc_j holds whatever k_j is
+    static bool split_linear(const ExprP& c, ExprP& k, int& q) {
+        if (c->op == Op::Var && c->vk == VarKind::Process) {
+            k = mk_const(1.0);
+            q = c->idx;
+            return true;
+        }
+        if (c->op != Op::Mul) return false;
+        const ExprP& a = c->args[0];
+        const ExprP& b = c->args[1];
+        if (b->op == Op::Var && b->vk == VarKind::Process) { k = a; q = b->idx; return true; }
+        if (a->op == Op::Var && a->vk == VarKind::Process) { k = b; q = a->idx; return true; }
+        return false;
+    }
+
+    // Euler update of process p.  FP64 keeps the reference's term order
+    // (val += c * inc per term).  FP32 factors coefficients k_j * X_q out of
+    // the sum: X_q * (sum_j k_j inc_j), one FMA per term instead of two
+    // operations; the value changes only by rounding.
+    void euler_update(Out& o, int p, const std::string& procset) const {
+        o.l(R + " " + V("N", p) + " = " + V("X", p) + ";");
+        const auto& terms = u.procs[p].terms;
+        if (!f32) {
+            for (const auto& t : terms)
+                o.l(V("N", p) + " = " + V("N", p) + " + " + ex(t.coef, procset, "tc") + " * " + inc(t) + ";");
+            return;
+        }
+        std::vector<int> groups;
+        std::vector<std::vector<std::pair<ExprP, std::string>>> gterms;
+        for (const auto& t : terms) {
+            ExprP k;
+            int q;
+            if (split_linear(t.coef, k, q)) {
+                auto it = std::find(groups.begin(), groups.end(), q);
+                size_t gi = it - groups.begin();
+                if (it == groups.end()) { groups.push_back(q); gterms.emplace_back(); }
+                gterms[gi].push_back({k, inc(t)});
+            } else {
+                o.l(V("N", p) + " = " + V("N", p) + " + " + ex(t.coef, procset, "tc") + " * " + inc(t) + ";");
+            }
+        }
+        for (size_t g = 0; g < groups.size(); ++g) {
+            const std::string acc = V("acc" + S(p) + "_", (int)g);
+            o.l(R + " " + acc + " = " + L(0.0) + ";");
+            for (const auto& kt : gterms[g]) o.l(acc + " = " + acc + " + " + ex(kt.first, procset, "tc") + " * " + kt.second + ";");
+            o.l(V("N", p) + " = " + V("N", p) + " + " + V(procset, groups[g]) + " * " + acc + ";");
+        }
+    }
+
+    // ---- one step, reference semantics ---------------------------------
     void step_reference(Out& o) const {
         if (sp.scheme == SCHEME_EULER) {
             // cache refresh at t when no algebraic process left it at t
             if (!has_alg())
-                for (int p : u.levy) o.l("C" + S(p) + " = X" + S(p) + ";");
+                for (int p : u.levy) o.l(V("C", p) + " = " + V("X", p) + ";");
             poisson(o, "C", "tc");
-            for (int p : u.levy) {
-                o.l(R + " N" + S(p) + " = X" + S(p) + ";");
-                for (const auto& t : u.procs[p].terms)
-                    o.l("N" + S(p) + " = N" + S(p) + " + " + ex(t.coef, "C", "tc") + " * " + inc(t) + ";");
-            }
+            for (int p : u.levy) euler_update(o, p, "C");
             if (has_alg()) {
                 // refresh at t+1 before any algebraic slot of t+1 is written
-                for (int p : u.levy) o.l("C" + S(p) + " = N" + S(p) + ";");
-                for (int q : u.alg) o.l("C" + S(q) + " = " + L(0.0) + ";");
-                for (int q : u.alg) o.l(R + " N" + S(q) + " = " + ex(u.procs[q].alg, "C", "tn") + ";");
+                for (int p : u.levy) o.l(V("C", p) + " = " + V("N", p) + ";");
+                for (int q : u.alg) o.l(V("C", q) + " = " + L(0.0) + ";");
+                for (int q : u.alg) o.l(R + " " + V("N", q) + " = " + ex(u.procs[q].alg, "C", "tn") + ";");
             }
         } else {
-            o.l("const " + R + " sk = " + sk_expr() + ";");
+            o.l("const " + R + " " + V("sk") + " = " + sk_expr() + ";");
             poisson(o, "C", "tc");
             for (int p : u.levy) {
                 const auto& terms = u.procs[p].terms;
+                const std::string cp = "c" + S(p) + "_";
                 for (size_t j = 0; j < terms.size(); ++j)
-                    o.l("const " + R + " c" + S(p) + "_" + S((int)j) + " = " + ex(terms[j].coef, "C", "tc") + ";");
-                o.l(R + " k1_" + S(p) + " = " + L(0.0) + ";");
+                    o.l("const " + R + " " + V(cp, (int)j) + " = " + ex(terms[j].coef, "C", "tc") + ";");
+                o.l(R + " " + V("k1_", p) + " = " + L(0.0) + ";");
                 for (size_t j = 0; j < terms.size(); ++j)
-                    o.l("k1_" + S(p) + " = k1_" + S(p) + " + c" + S(p) + "_" + S((int)j) + " * " + inc(terms[j]) + ";");
-                o.l(R + " pe" + S(p) + " = " + L(0.0) + ";");
+                    o.l(V("k1_", p) + " = " + V("k1_", p) + " + " + V(cp, (int)j) + " * " + inc(terms[j]) + ";");
+                o.l(R + " " + V("pe", p) + " = " + L(0.0) + ";");
                 for (size_t j = 0; j < terms.size(); ++j)
                     if (terms[j].kind == IncKind::Dw)
-                        o.l("pe" + S(p) + " = pe" + S(p) + " + c" + S(p) + "_" + S((int)j) + " * sk * sdt;");
+                        o.l(V("pe", p) + " = " + V("pe", p) + " + " + V(cp, (int)j) + " * " + V("sk") + " * sdt;");
             }
-            for (int p : u.levy) o.l("C" + S(p) + " = X" + S(p) + " + k1_" + S(p) + " + pe" + S(p) + ";");
-            for (int q : u.alg) o.l("C" + S(q) + " = " + L(0.0) + ";");
+            for (int p : u.levy)
+                o.l(V("C", p) + " = " + V("X", p) + " + " + V("k1_", p) + " + " + V("pe", p) + ";");
+            for (int q : u.alg) o.l(V("C", q) + " = " + L(0.0) + ";");
             for (int p : u.levy) {
                 const auto& terms = u.procs[p].terms;
-                o.l(R + " k2_" + S(p) + " = " + L(0.0) + ";");
+                o.l(R + " " + V("k2_", p) + " = " + L(0.0) + ";");
                 for (size_t j = 0; j < terms.size(); ++j)
-                    o.l("k2_" + S(p) + " = k2_" + S(p) + " + " + ex(terms[j].coef, "C", "tn") + " * " + inc(terms[j]) + ";");
-                o.l(R + " N" + S(p) + " = X" + S(p) + " + " + L(0.5) + " * (k1_" + S(p) + " + k2_" + S(p) + ");");
+                    o.l(V("k2_", p) + " = " + V("k2_", p) + " + " + ex(terms[j].coef, "C", "tn") + " * " + inc(terms[j]) + ";");
+                o.l(R + " " + V("N", p) + " = " + V("X", p) + " + " + L(0.5) + " * (" + V("k1_", p) + " + " + V("k2_", p) + ");");
             }
-            for (int q : u.alg) o.l(R + " N" + S(q) + " = " + ex(u.procs[q].alg, "C", "tn") + ";");
+            for (int q : u.alg) o.l(R + " " + V("N", q) + " = " + ex(u.procs[q].alg, "C", "tn") + ";");
         }
-        for (int p = 0; p < P; ++p) o.l("X" + S(p) + " = N" + S(p) + ";");
+        for (int p = 0; p < P; ++p) o.l(V("X", p) + " = " + V("N", p) + ";");
     }
 
     // ---- one step, textbook semantics ---------------------------------
     void settle_alg_textbook(Out& o) const {
         if (!has_alg()) return;
-        for (int q : u.alg) o.l(R + " N" + S(q) + " = X" + S(q) + ";");
-        for (int q : u.alg)
-            o.l("N" + S(q) + " = " + ex(u.procs[q].alg, "N", "tn") + ";");
+        for (int q : u.alg) o.l(R + " " + V("N", q) + " = " + V("X", q) + ";");
+        for (int q : u.alg) o.l(V("N", q) + " = " + ex(u.procs[q].alg, "N", "tn") + ";");
     }
     void step_textbook(Out& o) const {
+        // the Poisson intensity reads C, which is the true state here
+        for (int p = 0; p < P; ++p) o.l(V("C", p) + " = " + V("X", p) + ";");
         if (sp.scheme == SCHEME_EULER) {
-            poisson(o, "X", "tc");
-            for (int p : u.levy) {
-                o.l(R + " N" + S(p) + " = X" + S(p) + ";");
-                for (const auto& t : u.procs[p].terms)
-                    o.l("N" + S(p) + " = N" + S(p) + " + " + ex(t.coef, "X", "tc") + " * " + inc(t) + ";");
-            }
+            poisson(o, "C", "tc");
+            for (int p : u.levy) euler_update(o, p, "X");
             settle_alg_textbook(o);
         } else {
-            o.l("const " + R + " sk = " + sk_expr() + ";");
-            poisson(o, "X", "tc");
+            o.l("const " + R + " " + V("sk") + " = " + sk_expr() + ";");
+            poisson(o, "C", "tc");
             for (int p : u.levy) {
                 const auto& terms = u.procs[p].terms;
-                o.l(R + " k1_" + S(p) + " = " + L(0.0) + ";");
-                o.l(R + " pe" + S(p) + " = " + L(0.0) + ";");
+                const std::string cp = "c" + S(p) + "_";
+                o.l(R + " " + V("k1_", p) + " = " + L(0.0) + ";");
+                o.l(R + " " + V("pe", p) + " = " + L(0.0) + ";");
                 for (size_t j = 0; j < terms.size(); ++j) {
-                    o.l("const " + R + " c" + S(p) + "_" + S((int)j) + " = " + ex(terms[j].coef, "X", "tc") + ";");
-                    o.l("k1_" + S(p) + " = k1_" + S(p) + " + c" + S(p) + "_" + S((int)j) + " * " + inc(terms[j]) + ";");
+                    o.l("const " + R + " " + V(cp, (int)j) + " = " + ex(terms[j].coef, "X", "tc") + ";");
+                    o.l(V("k1_", p) + " = " + V("k1_", p) + " + " + V(cp, (int)j) + " * " + inc(terms[j]) + ";");
                     if (terms[j].kind == IncKind::Dw)
-                        o.l("pe" + S(p) + " = pe" + S(p) + " + c" + S(p) + "_" + S((int)j) + " * sk * sdt;");
+                        o.l(V("pe", p) + " = " + V("pe", p) + " + " + V(cp, (int)j) + " * " + V("sk") + " * sdt;");
                 }
             }
             for (int p = 0; p < P; ++p) {
-                if (u.procs[p].levy) o.l("const " + R + " PB" + S(p) + " = X" + S(p) + " + k1_" + S(p) + " + pe" + S(p) + ";");
-                else o.l("const " + R + " PB" + S(p) + " = X" + S(p) + ";");
+                if (u.procs[p].levy)
+                    o.l("const " + R + " " + V("PB", p) + " = " + V("X", p) + " + " + V("k1_", p) + " + " + V("pe", p) + ";");
+                else
+                    o.l("const " + R + " " + V("PB", p) + " = " + V("X", p) + ";");
             }
             for (int p : u.levy) {
                 const auto& terms = u.procs[p].terms;
-                o.l(R + " k2_" + S(p) + " = " + L(0.0) + ";");
+                o.l(R + " " + V("k2_", p) + " = " + L(0.0) + ";");
                 for (size_t j = 0; j < terms.size(); ++j)
-                    o.l("k2_" + S(p) + " = k2_" + S(p) + " + " + ex(terms[j].coef, "PB", "tn") + " * " + inc(terms[j]) + ";");
-                o.l(R + " N" + S(p) + " = X" + S(p) + " + " + L(0.5) + " * (k1_" + S(p) + " + k2_" + S(p) + ");");
+                    o.l(V("k2_", p) + " = " + V("k2_", p) + " + " + ex(terms[j].coef, "PB", "tn") + " * " + inc(terms[j]) + ";");
+                o.l(R + " " + V("N", p) + " = " + V("X", p) + " + " + L(0.5) + " * (" + V("k1_", p) + " + " + V("k2_", p) + ");");
             }
             settle_alg_textbook(o);
         }
-        for (int p = 0; p < P; ++p) o.l("X" + S(p) + " = N" + S(p) + ";");
+        for (int p = 0; p < P; ++p) o.l(V("X", p) + " = " + V("N", p) + ";");
+    }
+
+    void step(Out& o) const {
+        if (sp.semantics == SEM_TEXTBOOK) step_textbook(o);
+        else step_reference(o);
     }
 
     void store(Out& o, const std::string& tidx) const {
-        if (!sp.store_output) return;
+        if (!sp.store_output || mode != Mode::Forward) return;
         o.l("{ const int slot = __ldg(&a.out_tidx[" + tidx + "]);");
-        o.l("  if (slot >= 0 && active) {");
-        o.l("    " + R + "* dst = OUT + ((sde_u64)rep * a.n_out + slot) * (sde_u64)" + S(P) + " * a.n_paths + i;");
+        o.l("  if (slot >= 0 && " + V("active") + ") {");
+        o.l("    " + R + "* dst = OUT + ((sde_u64)rep * a.n_out + slot) * (sde_u64)" + S(P) + " * a.n_paths + " + V("i") + ";");
         for (int p = 0; p < P; ++p)
-            o.l("    dst[(sde_u64)" + S(p) + " * a.n_paths] = X" + S(p) + ";");
+            o.l("    dst[(sde_u64)" + S(p) + " * a.n_paths] = " + V("X", p) + ";");
         o.l("  } }");
     }
 
-    void prologue(Out& o) const {
-        o.l("const int lane = threadIdx.x & 31;");
-        o.l("const sde_u64 i = (sde_u64)blockIdx.x * blockDim.x + threadIdx.x;");
-        o.l("const int rep = blockIdx.y;");
-        o.l("const bool active = i < a.n_paths;");
-        o.l("const sde_u64 scen = a.path_base + (sde_u64)rep * a.n_paths + i;");
-        o.l("const int n_steps = a.T - 1;");
-        o.l("(void)lane; (void)scen;");
-        for (int k = 0; k < (int)u.params.size(); ++k)
-            o.l("const " + R + " PR" + S(k) + " = (" + R + ")__ldg(&a.params[" + S(k) + "]);");
-        for (int p = 0; p < P; ++p) o.l(R + " X" + S(p) + " = (" + R + ")__ldg(&a.x0[" + S(p) + "]);");
-        for (int p = 0; p < P; ++p) o.l(R + " C" + S(p) + " = X" + S(p) + ";");
-        if (sp.store_output) o.l(R + "* OUT = (" + R + "*)a.out;");
-        if (uses_chacha()) o.l("sde_u32 key[8]; sde_seed_from_u64(a.seed + scen, key);");
-        if (sp.rng == RNG_SOBOL && sp.scramble == SCRAMBLE_SHIFT)
-            o.l("const sde_u32 G = sde_gray((sde_u32)(scen + 5ull));");
-        if (sp.rng == RNG_SOBOL && sp.scramble == SCRAMBLE_XOR) {
-            o.l("const sde_u32 Gx = sde_gray((sde_u32)i);");
-            o.l("const sde_u32 L = Gx & 31u, H = Gx >> 5;");
-            o.l("const sde_u32* mask_rep = a.masks ? a.masks + (sde_u64)rep * a.mask_stride : nullptr;");
-            o.l("int hchunk = -1; sde_u32 hval = 0u;");
+    // ---- per-lane state --------------------------------------------------
+    void lane_prologue(Out& o) const {
+        if (mode == Mode::Forward) {
+            o.l("const sde_u64 " + V("i") + " = base + " + S(0) + "ull + (sde_u64)" + (sfx.empty() ? "0" : sfx.substr(1)) +
+                " * blockDim.x + threadIdx.x;");
+            o.l("const bool " + V("active") + " = " + V("i") + " < a.n_paths;");
+            o.l("const sde_u64 " + V("scen") + " = a.path_base + (sde_u64)rep * a.n_paths + " + V("i") + ";");
+            for (int p = 0; p < P; ++p) o.l(R + " " + V("X", p) + " = (" + R + ")__ldg(&a.x0[" + S(p) + "]);");
+        } else {
+            o.l("const sde_u64 " + V("i") + " = first + (sde_u64)" + (sfx.empty() ? "0" : sfx.substr(1)) +
+                " * blockDim.x + threadIdx.x;");
+            o.l("const bool " + V("active") + " = " + V("i") + " < in.n_paths;");
+            o.l("const sde_u64 " + V("scen") + " = " + V("i") + ";");
+            for (int p = 0; p < P; ++p) o.l(R + " " + V("X", p) + " = (" + R + ")__ldg(&a.x0[in.x0_off + " + S(p) + "]);");
+        }
+        o.l("(void)" + V("scen") + ";");
+        for (int p = 0; p < P; ++p) o.l(R + " " + V("C", p) + " = " + V("X", p) + ";");
+        const std::string seed = mode == Mode::Forward ? "a.seed" : "in.seed";
+        if (uses_chacha()) o.l("sde_u32 " + V("key") + "[8]; sde_seed_from_u64(" + seed + " + " + V("scen") + ", " + V("key") + ");");
+        if (shiftm()) o.l("const sde_u32 " + V("G") + " = sde_gray((sde_u32)(" + V("scen") + " + 5ull));");
+        if (xorm()) {
+            o.l("const sde_u32 " + V("Gx") + " = sde_gray((sde_u32)" + V("i") + ");");
+            o.l("const sde_u32 " + V("L") + " = " + V("Gx") + " & 31u, " + V("H") + " = " + V("Gx") + " >> 5;");
+            o.l("int " + V("hchunk") + " = -1; sde_u32 " + V("hval") + " = 0u;");
         }
     }
 
-    void time_loop(Out& o, bool textbook) const {
+    void shared_prologue(Out& o) const {
+        o.l("const int lane = threadIdx.x & 31;");
+        o.l("(void)lane;");
+        if (mode == Mode::Forward) {
+            o.l("const int rep = blockIdx.y;");
+            o.l("const sde_u64 base = (sde_u64)blockIdx.x * blockDim.x * " + S(ppt) + "ull;");
+            o.l("const int n_steps = a.T - 1;");
+            for (int k = 0; k < (int)u.params.size(); ++k)
+                o.l("const " + R + " PR" + S(k) + " = (" + R + ")__ldg(&a.params[" + S(k) + "]);");
+            if (sp.store_output) o.l(R + "* OUT = (" + R + "*)a.out;");
+            if (xorm()) o.l("const sde_u32* mask_rep = a.masks ? a.masks + (sde_u64)rep * a.mask_stride : nullptr;");
+        } else {
+            o.l("const int n_steps = in.n_steps;");
+            o.l("const " + R + " bdt = (" + R + ")in.dt" + (f32 ? "_f" : "") + ";");
+            o.l("const " + R + " bsdt = (" + R + ")in.sdt" + (f32 ? "_f" : "") + ";");
+            for (int k = 0; k < (int)u.params.size(); ++k)
+                o.l("const " + R + " PR" + S(k) + " = (" + R + ")__ldg(&a.params[in.par_off + " + S(k) + "]);");
+        }
+    }
+
+    void step_header(Out& o) const {
+        if (mode == Mode::Forward) {
+            o.l("const " + R + " tc = " + T("times") + ";");
+            o.l("const " + R + " tn = " + T("times", "t + 1") + ";");
+            o.l("const " + R + " dt = " + T("dts") + ";");
+            o.l("const " + R + " sdt = " + T("sqrt_dts") + ";");
+        } else {
+            o.l("const " + R + " tc = (" + R + ")t * bdt;");
+            o.l("const " + R + " tn = (" + R + ")(t + 1) * bdt;");
+            o.l("const " + R + " dt = bdt;");
+            o.l("const " + R + " sdt = bsdt;");
+        }
+        o.l("(void)tc; (void)tn; (void)dt; (void)sdt;");
+    }
+
+    void time_loop(Out& o) {
         const int U = group();
-        const int nblocks = uses_chacha() ? (U * NI) / 8 : 0;
+        const int nblocks = uses_chacha() ? (U * NI) / 8 : (xorm() ? (U * NI) / 32 : 0);
         o.l("for (int t0 = 0; t0 < n_steps; t0 += " + S(U) + ") {");
         o.ind++;
         if (uses_chacha()) {
             o.l("const sde_u64 blk0 = ((sde_u64)t0 * " + S(NI) + "ull) / 8ull;");
-            for (int b = 0; b < nblocks; ++b) o.l("sde_u32 B" + S(b) + "[16];");
+            for (int j = 0; j < ppt; ++j) {
+                lane(j);
+                for (int b = 0; b < nblocks; ++b) o.l("sde_u32 " + V("B", b) + "[16];");
+            }
         }
-        std::vector<bool> done(std::max(1, nblocks), false);
+        if (xorm()) {
+            // the group starts at dimension t0*NI, a multiple of 32
+            o.l("const int chunk0 = (t0 * " + S(NI) + ") >> 5;");
+            for (int j = 0; j < ppt; ++j) {
+                lane(j);
+                o.l("const sde_u32* " + V("LOp") + " = a.sobol_lo + (sde_u64)t0 * " + S(NI * 32) + "u + " + V("L") + ";");
+                for (int c = 0; c < nblocks; ++c) o.l("sde_u32 " + V("hv", c) + ";");
+            }
+        }
+        std::vector<std::vector<bool>> done(ppt, std::vector<bool>(std::max(1, nblocks), false));
         for (int g = 0; g < U; ++g) {
             o.l("{ const int t = t0 + " + S(g) + ";");
             o.l("if (t < n_steps) {");
             o.ind++;
-            o.l("const " + R + " tc = " + T("times") + ";");
-            o.l("const " + R + " tn = (" + R + ")__ldg(&a.times" + std::string(f32 ? "_f" : "") + "[t + 1]);");
-            o.l("const " + R + " dt = " + T("dts") + ";");
-            o.l("const " + R + " sdt = " + T("sqrt_dts") + ";");
-            o.l("(void)tc; (void)tn; (void)dt; (void)sdt;");
-            uniforms(o, g, done);
-            wiener(o);
-            if (textbook) step_textbook(o);
-            else step_reference(o);
-            store(o, "t + 1");
+            step_header(o);
+            for (int j = 0; j < ppt; ++j) {
+                lane(j);
+                o.l("{");
+                o.ind++;
+                uniforms(o, g, done[j]);
+                wiener(o, xorm() && f32);
+                step(o);
+                store(o, "t + 1");
+                o.ind--;
+                o.l("}");
+            }
             o.ind--;
             o.l("} }");
         }
         o.ind--;
         o.l("}");
+        lane(0);
     }
 
-    void epilogue(Out& o) const {
+    // payoff sums: fs[k], fq[k] (this thread's lanes)
+    void payoffs(Out& o, int K) {
+        const std::string tT = mode == Mode::Forward ? "(" + R + ")__ldg(&a.times[a.T - 1])"
+                                                     : "(" + R + ")n_steps * bdt";
+        o.l("const " + R + " tT = " + tT + "; (void)tT;");
+        for (int j = 0; j < ppt; ++j) {
+            lane(j);
+            for (int k = 0; k < (int)sp.payoffs.size(); ++k) {
+                o.l("{ const double v = " + V("active") + " ? (double)(" + ex(sp.payoffs[k], "X", "tT") + ") : 0.0;");
+                o.l("  fs[" + S(k) + "] += v; fq[" + S(k) + "] += v * v; }");
+            }
+        }
+        lane(0);
+        (void)K;
+    }
+
+    std::string forward(const std::string& name) {
+        mode = Mode::Forward;
         const int K = (int)sp.payoffs.size();
-        if (K == 0) return;
-        o.l("const " + R + " tT = (" + R + ")__ldg(&a.times[a.T - 1]);");
-        o.l("double f[" + S(K) + "];");
-        for (int k = 0; k < K; ++k)
-            o.l("f[" + S(k) + "] = active ? (double)(" + ex(sp.payoffs[k], "X", "tT") + ") : 0.0;");
-        o.l("sde_block_reduce_store<" + S(K) + ">(f, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " + S(K) + "u) * 4u);");
+        Out o;
+        o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
+        o.ind++;
+        shared_prologue(o);
+        for (int j = 0; j < ppt; ++j) {
+            lane(j);
+            lane_prologue(o);
+            store(o, "0");
+        }
+        lane(0);
+        time_loop(o);
+        if (K > 0) {
+            o.l("double fs[" + S(K) + "] = {}, fq[" + S(K) + "] = {};");
+            payoffs(o, K);
+            o.l("sde_block_reduce_store<" + S(K) + ">(fs, fq, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " +
+                S(K) + "u) * 4u);");
+        }
+        o.ind--;
+        o.l("}");
+        return o.s.str();
+    }
+
+    // Device function of one template for the batched kernel.
+    std::string batch_template(const std::string& name, int K) {
+        mode = Mode::Batch;
+        Out o;
+        o.l("static __device__ __forceinline__ void " + name +
+            "(const sde_batch_inst& in, sde_u64 first, const sde_batch_args& a, double (&fs)[" + S(K) +
+            "], double (&fq)[" + S(K) + "]) {");
+        o.ind++;
+        shared_prologue(o);
+        for (int j = 0; j < ppt; ++j) {
+            lane(j);
+            lane_prologue(o);
+        }
+        lane(0);
+        time_loop(o);
+        payoffs(o, K);
+        o.ind--;
+        o.l("}");
+        return o.s.str();
     }
 
     // ---- adjoint ---------------------------------------------------------
-    // Uniforms by random access (any step order): ChaCha blocks are cached
-    // per thread, Sobol points are direct.
-    void uniforms_ra(Out& o) const {
-        for (int k = 0; k < NI; ++k) {
-            const std::string K = S(k);
-            if (uses_chacha()) {
-                o.l("sde_u64 r" + K + ";");
-                o.l("{ const sde_u64 pos = (sde_u64)t * " + S(NI) + "ull + " + K + "ull;");
-                o.l("  if ((pos >> 3) != cblk) { cblk = pos >> 3; sde_chacha8_block(key, cblk, CB); }");
-                o.l("  const int w = (int)(pos & 7ull) * 2; r" + K + " = sde_pair(CB[w], CB[w + 1]); }");
-            }
-            if (sp.rng == RNG_PSEUDO) {
-                if (!f32) o.l("const double u" + K + " = sde_u64_to_f64(r" + K + ");");
-                else o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_u53(r" + K + " >> 11, q" + K + ", up" + K + ", gt" + K + ");");
-            } else if (sp.scramble == SCRAMBLE_SHIFT) {
-                o.l("const sde_u32 x" + K + " = sde_sobol_direct(a.sobol_v, t * " + S(NI) + " + " + K + ", G);");
-                if (!f32) {
-                    o.l("const double v" + K + " = (double)x" + K + " * 0x1p-32 + sde_u64_to_f64(r" + K + ");");
-                    o.l("const double u" + K + " = v" + K + " - trunc(v" + K + ");");
-                } else {
-                    o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_u53(sde_shift_u53(x" + K + ", r" + K + "), q" + K + ", up" + K + ", gt" + K + ");");
-                }
-            } else {
-                o.l("const int d" + K + " = t * " + S(NI) + " + " + K + ";");
-                o.l("if ((d" + K + " >> 5) != hchunk) { hchunk = d" + K + " >> 5; hval = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, hchunk, H, lane); }");
-                o.l("const sde_u32 y" + K + " = __shfl_sync(0xffffffffu, hval, d" + K + " & 31) ^ __ldg(&a.sobol_lo[(sde_u64)d" + K + " * 32u + L]);");
-                if (!f32) o.l("const double u" + K + " = ((double)y" + K + " + 0.5) * 0x1p-32;");
-                else o.l("float q" + K + "; bool up" + K + ", gt" + K + "; sde_tail_xor(y" + K + ", q" + K + ", up" + K + ", gt" + K + ");");
-            }
-        }
-    }
-
-    void step_header(Out& o) const {
-        o.l("const " + R + " tc = " + T("times") + ";");
-        o.l("const " + R + " tn = (" + R + ")__ldg(&a.times" + std::string(f32 ? "_f" : "") + "[t + 1]);");
-        o.l("const " + R + " dt = " + T("dts") + ";");
-        o.l("const " + R + " sdt = " + T("sqrt_dts") + ";");
-        o.l("(void)tc; (void)tn; (void)dt; (void)sdt;");
-    }
-
-    // increment k of a stochastic index as stored for the reverse sweep
     std::string inc_store_name(int k) const {
-        return u.token_kind[k] == IncKind::Dw ? "w" + S(k) : "n" + S(k);
+        return u.token_kind[k] == IncKind::Dw ? V("w", k) : V("n", k);
     }
 
-    std::string adjoint(const std::string& name) const {
+    std::string adjoint(const std::string& name) {
         // Pathwise adjoint of Euler-Maruyama: X' = X + sum_j c_j(t, X, theta) inc_j,
         // lambda_t = lambda_{t+1} + sum_p lambda_{t+1,p} sum_j dc_pj/dX inc_j,
         // g_theta += sum_p lambda_{t+1,p} sum_j dc_pj/dtheta inc_j.  Increments
         // are held fixed (common random numbers); jump counts are piecewise
         // constant in the parameters.
+        mode = Mode::Forward;
+        lane(0);
         const int E = sp.ckpt_every;
         const int K = (int)sp.payoffs.size();
         const int GP = (int)sp.grad_params.size(), GX = (int)sp.grad_x0.size();
+        const int KT = K + GP + GX;
         Out o;
         o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
         o.ind++;
-        prologue(o);
+        o.l("const int lane = threadIdx.x & 31;");
+        o.l("(void)lane;");
+        o.l("const int rep = blockIdx.y;");
+        o.l("const sde_u64 base = (sde_u64)blockIdx.x * blockDim.x;");
+        o.l("const int n_steps = a.T - 1;");
+        for (int k = 0; k < (int)u.params.size(); ++k)
+            o.l("const " + R + " PR" + S(k) + " = (" + R + ")__ldg(&a.params[" + S(k) + "]);");
+        if (xorm()) o.l("const sde_u32* mask_rep = a.masks ? a.masks + (sde_u64)rep * a.mask_stride : nullptr;");
+        lane_prologue(o);
         if (uses_chacha()) o.l("sde_u64 cblk = ~0ull; sde_u32 CB[16];");
         o.l(R + "* CK = (" + R + "*)a.ckpt;");
         o.l("const sde_u64 ckrow = (sde_u64)rep * a.n_ckpt;");
@@ -480,9 +672,9 @@ struct Gen {
         o.l("}");
         // payoffs and the terminal adjoint of payoff 0
         o.l("const " + R + " tT = (" + R + ")__ldg(&a.times[a.T - 1]);");
-        o.l("double f[" + S(K + GP + GX) + "];");
+        o.l("double fs[" + S(KT) + "] = {}, fq[" + S(KT) + "] = {};");
         for (int k = 0; k < K; ++k)
-            o.l("f[" + S(k) + "] = active ? (double)(" + ex(sp.payoffs[k], "X", "tT") + ") : 0.0;");
+            o.l("fs[" + S(k) + "] = active ? (double)(" + ex(sp.payoffs[k], "X", "tT") + ") : 0.0;");
         for (int p = 0; p < P; ++p)
             o.l(R + " LA" + S(p) + " = " + ex(derivative(sp.payoffs[0], VarKind::Process, p), "X", "tT") + ";");
         for (int m = 0; m < GP; ++m)
@@ -536,7 +728,8 @@ struct Gen {
                         o.l("  LN" + S(q) + " += " + li + " * " + ex(derivative(c, VarKind::Process, q), "Y", "tc") + ";");
                 for (int m = 0; m < GP; ++m)
                     if (depends_on(c, VarKind::Param, sp.grad_params[m]))
-                        o.l("  GP" + S(m) + " += " + li + " * " + ex(derivative(c, VarKind::Param, sp.grad_params[m]), "Y", "tc") + ";");
+                        o.l("  GP" + S(m) + " += " + li + " * " +
+                            ex(derivative(c, VarKind::Param, sp.grad_params[m]), "Y", "tc") + ";");
                 o.l("}");
             }
         }
@@ -545,22 +738,11 @@ struct Gen {
         o.l("}");
         o.ind--;
         o.l("}");
-        for (int m = 0; m < GP; ++m) o.l("f[" + S(K + m) + "] = active ? (double)GP" + S(m) + " : 0.0;");
-        for (int x = 0; x < GX; ++x) o.l("f[" + S(K + GP + x) + "] = active ? (double)LA" + S(sp.grad_x0[x]) + " : 0.0;");
-        o.l("sde_block_reduce_store<" + S(K + GP + GX) + ">(f, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " + S(K + GP + GX) + "u) * 4u);");
-        o.ind--;
-        o.l("}");
-        return o.s.str();
-    }
-
-    std::string forward(const std::string& name) const {
-        Out o;
-        o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
-        o.ind++;
-        prologue(o);
-        store(o, "0");
-        time_loop(o, sp.semantics == SEM_TEXTBOOK);
-        epilogue(o);
+        for (int m = 0; m < GP; ++m) o.l("fs[" + S(K + m) + "] = active ? (double)GP" + S(m) + " : 0.0;");
+        for (int x = 0; x < GX; ++x) o.l("fs[" + S(K + GP + x) + "] = active ? (double)LA" + S(sp.grad_x0[x]) + " : 0.0;");
+        o.l("for (int k = 0; k < " + S(KT) + "; ++k) fq[k] = fs[k] * fs[k];");
+        o.l("sde_block_reduce_store<" + S(KT) + ">(fs, fq, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " +
+            S(KT) + "u) * 4u);");
         o.ind--;
         o.l("}");
         return o.s.str();
@@ -581,6 +763,7 @@ static std::string tag(const KernelSpec& s) {
     std::string r = s.scheme == SCHEME_RK ? "rk" : "euler";
     r += s.precision == PREC_FP32 ? "_fp32" : "_fp64";
     r += s.rng == RNG_PSEUDO ? "_pseudo" : (s.scramble == SCRAMBLE_XOR ? "_sobolxor" : "_sobolshift");
+    if (s.ppt > 1) r += "_ppt" + std::to_string(s.ppt);
     return r;
 }
 
@@ -591,7 +774,61 @@ std::string generate_source(const Universe& u, const KernelSpec& s) {
     Gen g(u, s);
     std::string src;
     src += g.forward(forward_kernel_name(s));
-    if (s.adjoint) src += "\n" + g.adjoint(adjoint_kernel_name(s));
+    if (s.adjoint) {
+        KernelSpec s1 = s;
+        s1.ppt = 1;
+        Gen ga(u, s1);
+        src += "\n" + ga.adjoint(adjoint_kernel_name(s));
+    }
+    return src;
+}
+
+std::string batch_kernel_name(int block, int ppt) {
+    return "sde_batch_b" + std::to_string(block) + "_p" + std::to_string(ppt);
+}
+
+std::string generate_batch_source(const std::vector<const Universe*>& us, const std::vector<KernelSpec>& specs,
+                                  const std::vector<std::pair<int, int>>& variants, int K) {
+    std::string src;
+    std::vector<int> ppts;
+    for (const auto& v : variants)
+        if (std::find(ppts.begin(), ppts.end(), v.second) == ppts.end()) ppts.push_back(v.second);
+    for (int ppt : ppts)
+        for (size_t t = 0; t < us.size(); ++t) {
+            KernelSpec s = specs[t];
+            s.ppt = ppt;
+            s.store_output = false;
+            Gen g(*us[t], s);
+            src += g.batch_template("sde_tmpl" + std::to_string(t) + "_p" + std::to_string(ppt), K) + "\n";
+        }
+    for (const auto& v : variants) {
+        const int block = v.first, ppt = v.second;
+        Out o;
+        o.l("extern \"C\" __global__ void __launch_bounds__(" + S(block) + ") " + batch_kernel_name(block, ppt) +
+            "(const sde_batch_args a) {");
+        o.ind++;
+        o.l("__shared__ int s_item;");
+        o.l("for (;;) {");
+        o.ind++;
+        o.l("if (threadIdx.x == 0) s_item = (int)atomicAdd(a.counter, 1u);");
+        o.l("__syncthreads();");
+        o.l("const int item = s_item;");
+        o.l("if (item >= a.n_items) break;");
+        o.l("const sde_batch_item it = a.items[item];");
+        o.l("const sde_batch_inst in = a.inst[it.inst];");
+        o.l("double fs[" + S(K) + "] = {}, fq[" + S(K) + "] = {};");
+        o.l("switch (in.tmpl) {");
+        for (size_t t = 0; t < us.size(); ++t)
+            o.l("case " + S((int)t) + ": sde_tmpl" + S((int)t) + "_p" + S(ppt) + "(in, it.first_path, a, fs, fq); break;");
+        o.l("default: break;");
+        o.l("}");
+        o.l("sde_block_reduce_store<" + S(K) + ">(fs, fq, a.item_partials + (sde_u64)item * " + S(K) + "u * 4u);");
+        o.ind--;
+        o.l("}");
+        o.ind--;
+        o.l("}");
+        src += o.s.str() + "\n";
+    }
     return src;
 }
 

@@ -23,6 +23,7 @@ struct KernelSpec {
     bool store_output = true;           // filtration slices selected by out_tidx
     std::vector<ExprP> payoffs;         // resolved estimator expressions
     int block = 256;
+    int ppt = 1;                        // paths per thread (independent chains)
     // adjoint: parameters and initial values to differentiate
     bool adjoint = false;
     std::vector<int> grad_params;       // parameter indices
@@ -40,5 +41,13 @@ std::string generate_source(const Universe& u, const KernelSpec& s);
 
 // Expression emitter, exposed for tests of the lowering.
 std::string emit_expression(const ExprP& e, bool fp32);
+
+// Batched instances: one device function per (template, paths-per-thread)
+// and one persistent work-queue kernel per (block, paths-per-thread)
+// variant, all estimating K payoff columns.
+std::string batch_kernel_name(int block, int ppt);
+std::string generate_batch_source(const std::vector<const Universe*>& templates,
+                                  const std::vector<KernelSpec>& specs,
+                                  const std::vector<std::pair<int, int>>& variants, int K);
 
 }  // namespace sde

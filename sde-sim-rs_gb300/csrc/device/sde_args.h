@@ -42,4 +42,35 @@ typedef struct sde_args {
     int pad1;
 } sde_args;
 
+/* ---- batched instances: many independent SDE instances in one persistent
+ *      launch.  Instance i runs n_steps uniform steps of size dt on its own
+ *      template (lowered universe), parameters and initial values. */
+typedef struct sde_batch_inst {
+    double dt, sdt;           /* step and its square root                       */
+    sde_u64 n_paths;          /* paths of this instance                         */
+    sde_u64 seed;             /* path s uses ChaCha8 seed_from_u64(seed + s)     */
+    float dt_f, sdt_f;
+    int tmpl;                 /* template (universe) index                      */
+    int n_steps;
+    int x0_off;               /* offset of the instance's x0 row                */
+    int par_off;              /* offset of the instance's parameter row         */
+} sde_batch_inst;
+
+typedef struct sde_batch_item {
+    sde_u64 first_path;       /* first path of the chunk                        */
+    int inst;                 /* instance                                       */
+    int pad;
+} sde_batch_item;
+
+typedef struct sde_batch_args {
+    const sde_batch_inst* inst;
+    const sde_batch_item* items;  /* chunks, longest instances first            */
+    const double* x0;
+    const double* params;
+    unsigned int* counter;        /* work-queue head, zeroed before each launch */
+    double* item_partials;        /* [n_items][K][4]                            */
+    int n_items;
+    int pad0;
+} sde_batch_args;
+
 #endif

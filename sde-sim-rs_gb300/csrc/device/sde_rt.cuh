@@ -146,6 +146,39 @@ SDE_DEV double sde_icdf_as26(double p) {
     return p < 0.5 ? -x : x;
 }
 
+SDE_DEV float sde_lg2_approx(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+SDE_DEV float sde_rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+SDE_DEV float sde_rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+/* AS 26.2.23 in FP32 straight from an XOR-scrambled Sobol word y, with
+ * p = (y + 0.5) 2^-32: q = min(p, 1-p) = (2 min(y, ~y) + 1) 2^-33 is exact
+ * before its one rounding, log2 q = lg2(2m+1) - 33 folds into one FMA with
+ * -2 ln 2, sqrt(a) = a * rsqrt(a) (a >= 2 ln 2 > 0), the rational term is
+ * one reciprocal, and the sign (negative for p < 0.5) is one xor. */
+SDE_DEV float sde_normal_xor(sde_u32 y) {
+    const sde_u32 s = (sde_u32)((int)y >> 31);  /* all ones when p >= 0.5 */
+    const sde_u32 m = y ^ s;                    /* min(y, ~y) */
+    const float lg = sde_lg2_approx(__uint2float_rn(2u * m + 1u));
+    const float a = fmaf(lg, -1.3862943611198906f, 45.747713916956393f);  /* -2 ln q */
+    const float t = a * sde_rsqrt_approx(a);
+    const float num = fmaf(fmaf(0.010328f, t, 0.802853f), t, 2.515517f);
+    const float den = fmaf(fmaf(fmaf(0.001308f, t, 0.189269f), t, 1.432788f), t, 1.0f);
+    const float x = fmaf(-num, sde_rcp_approx(den), t);
+    return __int_as_float(__float_as_int(x) ^ (~s & 0x80000000u));
+}
+
 /* The same rational approximation in FP32, from the exact tail q. */
 SDE_DEV float sde_icdf_as26_q(float q, bool up) {
     const float t = sqrtf(-2.0f * __logf(q));
@@ -226,14 +259,17 @@ SDE_DEV void sde_neumaier(double& s, double& c, double x) {
     s = t;
 }
 
+/* s[k], q[k]: this thread's sum and sum of squares of estimator k (a thread
+ * may own several paths). */
 template <int K>
-SDE_DEV void sde_block_reduce_store(const double (&f)[K], double* __restrict__ out) {
+SDE_DEV void sde_block_reduce_store(const double (&fs)[K], const double (&fq)[K],
+                                    double* __restrict__ out) {
     __shared__ double sm[K][32][2];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nw = (blockDim.x + 31) >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        double s = f[k], q = f[k] * f[k];
+        double s = fs[k], q = fq[k];
 #pragma unroll
         for (int o = 16; o; o >>= 1) {
             s += __shfl_down_sync(SDE_FULL_MASK, s, o);

@@ -262,7 +262,9 @@ static std::shared_ptr<Cubin> compile_cubin(const std::string& gen_src, bool fp3
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, src.c_str(), "sde_plan.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
         fail(SDE_ERR_COMPILE, "nvrtcCreateProgram failed");
-    std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device"};
+    // 177: runtime helpers a given plan does not call
+    std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device",
+                                     "--ptxas-options=-v", "--diag-suppress=177"};
     if (fp32) {
         opts.push_back("-ftz=true");
         opts.push_back("-prec-div=false");
@@ -375,6 +377,8 @@ static KernelSpec spec_from(const sde_options* o) {
     if (o->output < SDE_OUT_FULL || o->output > SDE_OUT_NONE) fail(SDE_ERR_INVALID, "unknown output mode");
     if (s.block % 32 != 0 || s.block > 1024) fail(SDE_ERR_INVALID, "block_size must be a multiple of 32 up to 1024");
     s.ckpt_every = o->ckpt_every > 0 ? o->ckpt_every : 19;
+    s.ppt = o->paths_per_thread > 0 ? o->paths_per_thread : 1;
+    if (s.ppt != 1 && s.ppt != 2 && s.ppt != 4) fail(SDE_ERR_INVALID, "paths_per_thread must be 1, 2 or 4");
     if (s.ckpt_every > 256) fail(SDE_ERR_INVALID, "ckpt_every must be at most 256");
     return s;
 }
@@ -438,7 +442,9 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         fail(SDE_ERR_UNSUPPORTED, "Sobol point index beyond 2^32");
     if (xorm && N > (1ull << 32)) fail(SDE_ERR_UNSUPPORTED, "more than 2^32 Sobol points per replicate");
     const int block = p->spec.block;
-    const uint64_t gx = (N + block - 1) / block;
+    // the adjoint kernel steps one path per thread
+    const uint64_t per_block = (uint64_t)block * (p->spec.adjoint ? 1 : p->spec.ppt);
+    const uint64_t gx = (N + per_block - 1) / per_block;
     if (gx > 0x7fffffffull) fail(SDE_ERR_INVALID, "too many paths for one launch");
 
     // output slots
@@ -760,6 +766,15 @@ int sde_plan_source(const sde_plan* p, char* buf, size_t n, size_t* needed) {
     });
 }
 
+int sde_plan_compile_log(const sde_plan* p, char* buf, size_t n, size_t* needed) {
+    return guarded([&] {
+        if (!p) fail(SDE_ERR_INVALID, "NULL plan");
+        const std::string& s = p->cubin->log;
+        if (needed) *needed = s.size() + 1;
+        if (buf && n) std::snprintf(buf, n, "%s", s.c_str());
+    });
+}
+
 int sde_run(sde_plan* p, const sde_run_args* a, sde_result** out) {
     return guarded([&] {
         if (!p || !a || !out) fail(SDE_ERR_INVALID, "NULL argument");
@@ -954,6 +969,314 @@ int sde_probe_sfu_peak(double* ops) {
     return guarded([&] {
         if (!ops) fail(SDE_ERR_INVALID, "NULL output");
         cuda_check(run_sfu_probe(ops), "SFU probe");
+    });
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched instances: one persistent work-queue kernel over many instances
+// ===========================================================================
+
+namespace sde {
+
+// candidate (block, paths per thread) shapes the autotuner times
+static const std::vector<std::pair<int, int>> kBatchVariants = {
+    {128, 1}, {256, 1}, {128, 2}, {256, 2}, {128, 4}};
+
+}  // namespace sde
+
+struct sde_batch {
+    std::vector<sde::Universe> u;
+    std::vector<sde::KernelSpec> specs;
+    int K = 0;
+    bool fp32 = true;
+    std::string source;
+    std::shared_ptr<sde::Cubin> cubin;
+    struct Dev {
+        cudaLibrary_t lib = nullptr;
+        std::vector<cudaKernel_t> kernels;  // per variant
+        std::vector<int> grid;              // persistent grid per variant
+    };
+    std::mutex mu;
+    std::map<int, Dev> dev;
+};
+
+struct sde_batch_job {
+    sde_batch* b = nullptr;
+    int n_inst = 0, n_items = 0, variant = 0;
+    uint64_t path_steps = 0;
+    sde::DBuf inst, items, x0, params, counter, item_partials, ranges, est;
+    sde::HBuf est_host;
+    sde_batch_args args{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+namespace sde {
+
+static sde_batch::Dev& batch_loaded(sde_batch* b) {
+    int dev = 0, sms = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> g(b->mu);
+    auto& D = b->dev[dev];
+    if (D.lib) return D;
+    cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    cuda_check(cudaLibraryLoadData(&D.lib, b->cubin->image.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
+               "cudaLibraryLoadData");
+    for (const auto& v : kBatchVariants) {
+        cudaKernel_t k;
+        cuda_check(cudaLibraryGetKernel(&k, D.lib, batch_kernel_name(v.first, v.second).c_str()),
+                   "cudaLibraryGetKernel");
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k, v.first, 0) != cudaSuccess ||
+            per_sm < 1) {
+            cudaGetLastError();
+            per_sm = 2048 / v.first;
+        }
+        D.kernels.push_back(k);
+        D.grid.push_back(per_sm * sms);
+    }
+    return D;
+}
+
+// Work items for one (block, ppt) shape: chunks of block*ppt paths, the
+// instances with the most steps first so the queue drains evenly.
+static void build_items(sde_batch_job* j, const sde_batch_instances& in, int variant, cudaStream_t s) {
+    const int chunk = kBatchVariants[variant].first * kBatchVariants[variant].second;
+    std::vector<int> order(in.n_instances);
+    for (int i = 0; i < in.n_instances; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return in.n_steps[a] > in.n_steps[b]; });
+    std::vector<sde_batch_item> items;
+    std::vector<int> ranges(2 * (size_t)in.n_instances);
+    for (int i : order) {
+        ranges[2 * i] = (int)items.size();
+        for (uint64_t f = 0; f < in.n_paths[i]; f += chunk) items.push_back({f, i, 0});
+        ranges[2 * i + 1] = (int)items.size();
+    }
+    j->n_items = (int)items.size();
+    j->variant = variant;
+    j->items = DBuf(std::max<size_t>(1, items.size()) * sizeof(sde_batch_item));
+    j->ranges = DBuf(ranges.size() * sizeof(int) + 8);
+    j->item_partials = DBuf(std::max<size_t>(1, items.size()) * j->b->K * 4 * 8);
+    if (!items.empty())
+        cuda_check(cudaMemcpyAsync(j->items.p, items.data(), items.size() * sizeof(sde_batch_item),
+                                   cudaMemcpyHostToDevice, s), "items H2D");
+    cuda_check(cudaMemcpyAsync(j->ranges.p, ranges.data(), ranges.size() * sizeof(int), cudaMemcpyHostToDevice, s),
+               "ranges H2D");
+    cuda_check(cudaStreamSynchronize(s), "items");
+    j->args.items = j->items.as<sde_batch_item>();
+    j->args.item_partials = j->item_partials.as<double>();
+    j->args.n_items = j->n_items;
+}
+
+static void batch_enqueue(sde_batch_job* j, cudaStream_t s) {
+    auto& D = batch_loaded(j->b);
+    cuda_check(cudaMemsetAsync(j->counter.p, 0, sizeof(unsigned), s), "queue reset");
+    void* kargs[] = {&j->args};
+    const auto& v = kBatchVariants[j->variant];
+    cuda_check(cudaLaunchKernel((const void*)D.kernels[j->variant], dim3((unsigned)D.grid[j->variant]),
+                                dim3(v.first), kargs, 0, s),
+               "batch kernel launch");
+    cuda_check(launch_reduce_ranges(j->item_partials.as<double>(), j->ranges.as<int>(), j->n_inst, j->b->K,
+                                    j->est.as<double>(), s),
+               "batch reduction");
+    cuda_check(cudaMemcpyAsync(j->est_host.p, j->est.p, (size_t)j->n_inst * j->b->K * 16, cudaMemcpyDeviceToHost, s),
+               "batch results D2H");
+}
+
+static float time_variant(sde_batch_job* j, cudaStream_t s) {
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cuda_check(cudaEventCreate(&e1), "event");
+    batch_enqueue(j, s);  // warm
+    float best = 1e30f;
+    for (int r = 0; r < 2; ++r) {
+        cuda_check(cudaEventRecord(e0, s), "event");
+        batch_enqueue(j, s);
+        cuda_check(cudaEventRecord(e1, s), "event");
+        cuda_check(cudaEventSynchronize(e1), "autotune run");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return best;
+}
+
+}  // namespace sde
+
+extern "C" {
+
+int sde_batch_create(const sde_plan* const* templates, int32_t n_templates, sde_batch** out) {
+    return guarded([&] {
+        if (!out || !templates || n_templates < 1) fail(SDE_ERR_INVALID, "need at least one template");
+        *out = nullptr;
+        auto b = std::make_unique<sde_batch>();
+        std::vector<const Universe*> us;
+        for (int t = 0; t < n_templates; ++t) {
+            const sde_plan* p = templates[t];
+            if (!p) fail(SDE_ERR_INVALID, "NULL template");
+            if (p->spec.rng != RNG_PSEUDO) fail(SDE_ERR_UNSUPPORTED, "batched templates use the pseudo-random streams");
+            if (p->spec.adjoint) fail(SDE_ERR_UNSUPPORTED, "batched templates are forward plans");
+            if (t > 0 && p->spec.precision != templates[0]->spec.precision)
+                fail(SDE_ERR_INVALID, "batched templates must share one precision");
+            if (p->spec.scheme == SCHEME_RK && p->u.n_stochastic() == 0)
+                fail(SDE_ERR_RNG_INDEX, "RNG Index 0 out of bounds (max 0)");
+            b->u.push_back(p->u);
+            b->specs.push_back(p->spec);
+            b->K = std::max(b->K, (int)p->spec.payoffs.size());
+        }
+        if (b->K < 1) fail(SDE_ERR_INVALID, "batched templates need at least one payoff");
+        for (auto& u : b->u) us.push_back(&u);
+        b->fp32 = templates[0]->spec.precision == PREC_FP32;
+        b->source = generate_batch_source(us, b->specs, kBatchVariants, b->K);
+        b->cubin = compile_cubin(b->source, b->fp32);
+        *out = b.release();
+    });
+}
+
+int sde_batch_destroy(sde_batch* b) {
+    return guarded([&] {
+        if (!b) return;
+        for (auto& kv : b->dev)
+            if (kv.second.lib) cudaLibraryUnload(kv.second.lib);
+        delete b;
+    });
+}
+
+int sde_batch_prepare(sde_batch* b, const sde_batch_instances* in, int32_t autotune, void* stream,
+                      sde_batch_job** out) {
+    return guarded([&] {
+        if (!b || !in || !out) fail(SDE_ERR_INVALID, "NULL argument");
+        if (in->struct_size != sizeof(sde_batch_instances)) fail(SDE_ERR_INVALID, "sde_batch_instances.struct_size mismatch");
+        *out = nullptr;
+        cudaStream_t s = (cudaStream_t)stream;
+        const int n = in->n_instances;
+        if (n < 1) fail(SDE_ERR_INVALID, "no instances");
+        auto j = std::make_unique<sde_batch_job>();
+        j->b = b;
+        j->n_inst = n;
+        std::vector<sde_batch_inst> hi(n);
+        int maxP = 1, maxK = 1;
+        for (auto& u : b->u) {
+            maxP = std::max(maxP, u.n_processes());
+            maxK = std::max(maxK, (int)u.params.size());
+        }
+        if (in->x0_stride < maxP && in->x0) fail(SDE_ERR_INVALID, "x0_stride is smaller than a template's process count");
+        for (int i = 0; i < n; ++i) {
+            const int t = in->template_id[i];
+            if (t < 0 || t >= (int)b->u.size()) fail(SDE_ERR_INVALID, "template_id out of range");
+            if (in->n_steps[i] < 1) fail(SDE_ERR_INVALID, "n_steps must be >= 1");
+            if (!(in->t_end[i] > 0)) fail(SDE_ERR_INVALID, "t_end must be positive");
+            if ((int)b->u[t].params.size() > in->param_stride)
+                fail(SDE_ERR_INVALID, "param_stride is smaller than a template's parameter count");
+            const double dt = in->t_end[i] / in->n_steps[i];
+            hi[i].dt = dt;
+            hi[i].sdt = std::sqrt(dt);
+            hi[i].dt_f = (float)dt;
+            hi[i].sdt_f = (float)std::sqrt(dt);
+            hi[i].n_paths = in->n_paths[i];
+            hi[i].seed = in->seed[i];
+            hi[i].tmpl = t;
+            hi[i].n_steps = in->n_steps[i];
+            hi[i].x0_off = i * in->x0_stride;
+            hi[i].par_off = i * in->param_stride;
+            j->path_steps += in->n_paths[i] * (uint64_t)in->n_steps[i];
+        }
+        const size_t nx = (size_t)n * std::max(1, in->x0_stride), np = (size_t)n * std::max(1, in->param_stride);
+        j->inst = DBuf(n * sizeof(sde_batch_inst));
+        j->x0 = DBuf(nx * 8);
+        j->params = DBuf(np * 8);
+        j->counter = DBuf(16);
+        j->est = DBuf((size_t)n * b->K * 16);
+        j->est_host = HBuf((size_t)n * b->K * 16);
+        std::vector<double> zx(nx, 0.0), zp(np, 0.0);
+        if (in->x0) std::copy(in->x0, in->x0 + (size_t)n * in->x0_stride, zx.begin());
+        if (in->params) std::copy(in->params, in->params + (size_t)n * in->param_stride, zp.begin());
+        cuda_check(cudaMemcpyAsync(j->inst.p, hi.data(), n * sizeof(sde_batch_inst), cudaMemcpyHostToDevice, s), "H2D");
+        cuda_check(cudaMemcpyAsync(j->x0.p, zx.data(), nx * 8, cudaMemcpyHostToDevice, s), "H2D");
+        cuda_check(cudaMemcpyAsync(j->params.p, zp.data(), np * 8, cudaMemcpyHostToDevice, s), "H2D");
+        j->args.inst = j->inst.as<sde_batch_inst>();
+        j->args.x0 = j->x0.as<double>();
+        j->args.params = j->params.as<double>();
+        j->args.counter = j->counter.as<unsigned>();
+        batch_loaded(b);
+        int best = 0;
+        if (autotune) {
+            float best_ms = 1e30f;
+            for (int v = 0; v < (int)kBatchVariants.size(); ++v) {
+                build_items(j.get(), *in, v, s);
+                const float ms = time_variant(j.get(), s);
+                if (ms < best_ms) { best_ms = ms; best = v; }
+            }
+        }
+        build_items(j.get(), *in, best, s);
+        // capture reset + persistent kernel + reduction + D2H in one graph
+        cudaStream_t cap = nullptr;
+        cuda_check(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
+        cuda_check(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+        try {
+            batch_enqueue(j.get(), cap);
+        } catch (...) {
+            cudaGraph_t g;
+            cudaStreamEndCapture(cap, &g);
+            cudaStreamDestroy(cap);
+            throw;
+        }
+        cuda_check(cudaStreamEndCapture(cap, &j->graph), "end capture");
+        cudaStreamDestroy(cap);
+        cuda_check(cudaGraphInstantiate(&j->exec, j->graph, 0), "graph instantiate");
+        cuda_check(cudaEventCreateWithFlags(&j->done, cudaEventDisableTiming), "event");
+        *out = j.release();
+    });
+}
+
+int sde_batch_job_run(sde_batch_job* j, void* stream) {
+    return guarded([&] {
+        if (!j) fail(SDE_ERR_INVALID, "NULL job");
+        cudaStream_t s = (cudaStream_t)stream;
+        cuda_check(cudaGraphLaunch(j->exec, s), "graph launch");
+        cuda_check(cudaEventRecord(j->done, s), "event");
+    });
+}
+
+int sde_batch_job_results(sde_batch_job* j, double* sum, double* sumsq) {
+    return guarded([&] {
+        if (!j) fail(SDE_ERR_INVALID, "NULL job");
+        cuda_check(cudaEventSynchronize(j->done), "batch execution");
+        const double* e = j->est_host.as<double>();
+        for (int i = 0; i < j->n_inst * j->b->K; ++i) {
+            if (sum) sum[i] = e[2 * i];
+            if (sumsq) sumsq[i] = e[2 * i + 1];
+        }
+    });
+}
+
+int sde_batch_job_info(const sde_batch_job* j, int32_t* block, int32_t* ppt, int32_t* n_items, uint64_t* path_steps,
+                       int32_t* n_payoffs) {
+    return guarded([&] {
+        if (!j) fail(SDE_ERR_INVALID, "NULL job");
+        if (block) *block = kBatchVariants[j->variant].first;
+        if (ppt) *ppt = kBatchVariants[j->variant].second;
+        if (n_items) *n_items = j->n_items;
+        if (path_steps) *path_steps = j->path_steps;
+        if (n_payoffs) *n_payoffs = j->b->K;
+    });
+}
+
+int sde_batch_job_destroy(sde_batch_job* j) {
+    return guarded([&] {
+        if (!j) return;
+        if (j->done) {
+            cudaEventSynchronize(j->done);
+            cudaEventDestroy(j->done);
+        }
+        if (j->exec) cudaGraphExecDestroy(j->exec);
+        if (j->graph) cudaGraphDestroy(j->graph);
+        delete j;
     });
 }
 

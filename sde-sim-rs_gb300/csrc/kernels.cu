@@ -72,6 +72,40 @@ cudaError_t launch_reduce_partials(const double* partials, int n_blocks, int K, 
     return cudaGetLastError();
 }
 
+__global__ void k_reduce_ranges(const double* __restrict__ partials, const int* __restrict__ ranges,
+                                int K, double* __restrict__ out) {
+    const int inst = blockIdx.x, k = blockIdx.y;
+    const int b0 = ranges[2 * inst], b1 = ranges[2 * inst + 1];
+    double s = 0.0, sc = 0.0, q = 0.0, qc = 0.0;
+    for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+        const double* p = partials + ((sde_u64)b * K + k) * 4;
+        merge_pair(s, sc, p[0], p[1]);
+        merge_pair(q, qc, p[2], p[3]);
+    }
+    __shared__ double sm[128][4];
+    sm[threadIdx.x][0] = s; sm[threadIdx.x][1] = sc;
+    sm[threadIdx.x][2] = q; sm[threadIdx.x][3] = qc;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            merge_pair(sm[threadIdx.x][0], sm[threadIdx.x][1], sm[threadIdx.x + h][0], sm[threadIdx.x + h][1]);
+            merge_pair(sm[threadIdx.x][2], sm[threadIdx.x][3], sm[threadIdx.x + h][2], sm[threadIdx.x + h][3]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[((sde_u64)inst * K + k) * 2 + 0] = sm[0][0] + sm[0][1];
+        out[((sde_u64)inst * K + k) * 2 + 1] = sm[0][2] + sm[0][3];
+    }
+}
+
+cudaError_t launch_reduce_ranges(const double* item_partials, const int* ranges, int n, int K,
+                                 double* out, cudaStream_t s) {
+    if (n == 0 || K == 0) return cudaSuccess;
+    k_reduce_ranges<<<dim3(n, K), 128, 0, s>>>(item_partials, ranges, K, out);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Long-format export: the filtration viewed as [rep][J][path] with
 // J = slot*P + p is transposed to [rep][path][J] through a 32x32 shared

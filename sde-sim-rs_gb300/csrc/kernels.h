@@ -17,6 +17,11 @@ cudaError_t launch_make_xor_masks(sde_u32* masks, int n_rep, int stride, sde_u64
 cudaError_t launch_reduce_partials(const double* partials, int n_blocks, int K, int n_rep,
                                    double* out, cudaStream_t s);
 
+// Item partials [n_items][K][4] -> per instance [n][K][2]; instance i owns
+// items ranges[2i] .. ranges[2i+1]-1.
+cudaError_t launch_reduce_ranges(const double* item_partials, const int* ranges, int n, int K,
+                                 double* out, cudaStream_t s);
+
 // Filtration [rep][slot][p][path] (f32 or f64) -> long rows ordered
 // (scenario, time, process) as in src/filtration.rs:81-116.
 cudaError_t launch_long_export(const void* vals, int elem_bytes, sde_u64 n_paths, int n_out, int P,

@@ -37,7 +37,7 @@ class Frame(dict):
 
     @property
     def height(self) -> int:
-        return len(next(iter(self.values()))) if self else 0
+        return len(next(iter(self.values()))) if dict.__len__(self) else 0
 
     def __len__(self):
         return self.height
@@ -219,6 +219,15 @@ class Plan:
         buf = C.create_string_buffer(need.value)
         N.check(N.lib().sde_plan_source(self._h, buf, need.value, None))
         return buf.value.decode()
+
+    @property
+    def compile_log(self) -> str:
+        """NVRTC / ptxas output of the lowering (registers, spills)."""
+        need = C.c_size_t()
+        N.check(N.lib().sde_plan_compile_log(self._h, None, 0, C.byref(need)))
+        buf = C.create_string_buffer(need.value)
+        N.check(N.lib().sde_plan_compile_log(self._h, buf, need.value, None))
+        return buf.value.decode(errors="replace")
 
     def index(self, name: str) -> int:
         idx = C.c_int32()

@@ -34,7 +34,7 @@ class Options(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("scheme", C.c_int32), ("rng", C.c_int32),
                 ("scramble", C.c_int32), ("precision", C.c_int32), ("semantics", C.c_int32),
                 ("output", C.c_int32), ("block_size", C.c_int32), ("ckpt_every", C.c_int32),
-                ("reserved", C.c_int32 * 7)]
+                ("paths_per_thread", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class RunArgs(C.Structure):
@@ -47,6 +47,13 @@ class RunArgs(C.Structure):
                 ("checkpoints", C.POINTER(C.c_int32)), ("n_checkpoints", C.c_int32),
                 ("stream", C.c_void_p), ("device_out", C.c_void_p),
                 ("device_out_bytes", C.c_uint64)]
+
+
+class BatchInstances(C.Structure):
+    _fields_ = [("struct_size", C.c_uint32), ("n_instances", C.c_int32),
+                ("template_id", C.c_void_p), ("n_steps", C.c_void_p), ("t_end", C.c_void_p),
+                ("n_paths", C.c_void_p), ("seed", C.c_void_p), ("x0", C.c_void_p),
+                ("x0_stride", C.c_int32), ("params", C.c_void_p), ("param_stride", C.c_int32)]
 
 
 class SdeError(RuntimeError):
@@ -76,6 +83,7 @@ SIGNATURES = {
     "sde_plan_process_index": ([C.c_void_p, C.c_char_p, C.POINTER(C.c_int32)], C.c_int),
     "sde_plan_stochastic_token": ([C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t], C.c_int),
     "sde_plan_source": ([C.c_void_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
+    "sde_plan_compile_log": ([C.c_void_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
     "sde_run": ([C.c_void_p, C.POINTER(RunArgs), C.POINTER(C.c_void_p)], C.c_int),
     "sde_simulate": ([C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_double), C.c_int32,
                       C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.c_int32, C.c_uint64,
@@ -90,6 +98,15 @@ SIGNATURES = {
     "sde_result_copy_values": ([C.c_void_p, C.c_void_p, C.c_int32], C.c_int),
     "sde_result_copy_long": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sde_result_estimates": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sde_batch_create": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
+    "sde_batch_destroy": ([C.c_void_p], C.c_int),
+    "sde_batch_prepare": ([C.c_void_p, C.POINTER(BatchInstances), C.c_int32, C.c_void_p,
+                           C.POINTER(C.c_void_p)], C.c_int),
+    "sde_batch_job_run": ([C.c_void_p, C.c_void_p], C.c_int),
+    "sde_batch_job_results": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sde_batch_job_info": ([C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                            C.POINTER(C.c_int32), C.POINTER(C.c_uint64), C.POINTER(C.c_int32)], C.c_int),
+    "sde_batch_job_destroy": ([C.c_void_p], C.c_int),
     "sde_kat_chacha8_u64": ([C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p], C.c_int),
     "sde_kat_sobol_points": ([C.c_int32, C.c_uint64, C.c_uint64, C.c_void_p], C.c_int),
     "sde_kat_icdf": ([C.c_void_p, C.c_uint64, C.c_void_p], C.c_int),

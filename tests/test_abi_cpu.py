@@ -59,8 +59,20 @@ def test_lowering_compiles(engine, scheme, rng, scramble, precision, semantics):
     assert "__global__" in src and "sde_step_" in src
     if precision == "fp32":
         # FP32 stepping: no double arithmetic in the step body
-        body = src.split("for (int t0 = 0;")[1].split("double f[")[0]
+        body = src.split("for (int t0 = 0;")[1].split("double fs[")[0]
         assert "double" not in body
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_degenerate_universes_compile(engine, precision):
+    # no stochastic term (RK panics only once a step runs), no Levy term,
+    # only algebraic processes, a process with no terms
+    for scheme in ("euler", "runge-kutta"):
+        engine.Plan(["dX = (0.1 * X) * dt"], scheme=scheme, precision=precision)
+        engine.Plan(["Y = 2 * t"], scheme=scheme, precision=precision)
+        engine.Plan(["dX = 3", "Y = X + 1"], scheme=scheme, precision=precision)
+    f = engine.Frame(a=np.arange(3))
+    assert len(f) == 3 and f.height == 3 and len(engine.Frame()) == 0
 
 
 def test_fasteval_operators_compile(engine):
@@ -147,3 +159,34 @@ def test_sobol_dimension_limit_message(engine):
     # before touching a device
     with pytest.raises(Exception, match="Joe-Kuo table has 21201"):
         p.run(np.arange(21203, dtype=np.float64), {"X": 1.0}, 4)
+
+
+def test_batch_lowering_compiles(engine):
+    from sde_sim_rs.batch import Batch
+    tg = engine.Plan(["dX = (mu * X) * dt + (sigma * X) * dW1"], params=["mu", "sigma"], payoffs=["X"],
+                     precision="fp32", output="none")
+    to = engine.Plan(["dX = (theta * (m - X)) * dt + (s) * dW1"], params=["theta", "m", "s"],
+                     payoffs=["X", "X^2"], precision="fp32", output="none", scheme="runge-kutta")
+    Batch([tg, to])
+    with pytest.raises(Exception, match="pseudo-random"):
+        Batch([engine.Plan(["dX = (0.1) * dW1"], payoffs=["X"], rng="sobol")])
+    with pytest.raises(ValueError, match="share one precision"):
+        Batch([tg, engine.Plan(["dX = (0.1) * dW1"], payoffs=["X"], precision="fp64")])
+
+
+@pytest.mark.parametrize("ppt", [2, 4])
+def test_paths_per_thread_lowering(engine, ppt):
+    from sde_sim_rs import _native as N
+    import ctypes as C
+    p = engine.Plan(["dv = (2 * (0.04 - max(v, 0))) * dt + (0.3 * max(v, 0)^0.5) * dW1",
+                     "dS = (0.03 * S) * dt + (-0.7 * max(v, 0)^0.5 * S) * dW1"], payoffs=["S"],
+                    rng="sobol", scramble="xor", precision="fp32", output="terminal")
+    src = p.source
+    assert "X1_1" not in src
+    opts = N.Options()
+    N.lib().sde_options_init(C.byref(opts))
+    opts.paths_per_thread = ppt
+    h = C.c_void_p()
+    N.check(N.lib().sde_plan_create(N.cstrs(["dX = (0.1 * X) * dW1"]), 1, N.cstrs([]), 0, N.cstrs(["X"]), 1,
+                                    C.byref(opts), C.byref(h)))
+    N.lib().sde_plan_destroy(h)

