@@ -78,8 +78,14 @@ typedef struct sde_options {
                                0 = 19                                      */
     int32_t paths_per_thread; /* independent paths a thread steps in
                                lockstep (1, 2 or 4), 0 = 1                 */
-    int32_t reserved[6];
+    int32_t icdf;           /* SDE_ICDF_*          default AS26            */
+    int32_t reserved[5];
 } sde_options;
+
+/* AS26: the reference's Abramowitz-Stegun 26.2.23 normal (|err| ~ 4.5e-4).
+ * ACCURATE: that value refined by Halley steps on Phi through erfc of the
+ *           exact tail probability (FP64: two steps, FP32: one).          */
+enum { SDE_ICDF_AS26 = 0, SDE_ICDF_ACCURATE = 1 };
 
 typedef struct sde_run_args {
     uint32_t struct_size;       /* sizeof(sde_run_args), set by sde_run_args_init */

@@ -46,7 +46,7 @@ class _Cfg(C.Structure):
     _fields_ = [("scheme", C.c_int), ("rng", C.c_int), ("scramble", C.c_int),
                 ("semantics", C.c_int), ("seed", C.c_uint64),
                 ("n_paths_per_replicate", C.c_uint64),
-                ("sobol_v", C.POINTER(C.c_uint32)), ("sobol_dims", C.c_int)]
+                ("sobol_v", C.POINTER(C.c_uint32)), ("sobol_dims", C.c_int), ("icdf", C.c_int)]
 
 
 _lib = None
@@ -89,6 +89,8 @@ def lib():
         L.orc_sobol_points.argtypes = [C.c_void_p, C.c_int, C.c_uint64, C.c_uint64, C.c_void_p]
         L.orc_icdf_as26.argtypes = [C.c_double]
         L.orc_icdf_as26.restype = C.c_double
+        L.orc_icdf_accurate.argtypes = [C.c_double]
+        L.orc_icdf_accurate.restype = C.c_double
         L.orc_poisson.argtypes = [C.c_double, C.c_double]
         L.orc_poisson.restype = C.c_uint64
         _lib = L
@@ -172,6 +174,10 @@ def xor_mask(seed: int, replicate: int, dim: int) -> int:
     return int(lib().orc_xor_mask(seed, replicate, dim))
 
 
+def icdf_accurate(p: float) -> float:
+    return lib().orc_icdf_accurate(p)
+
+
 def icdf_as26(p: float) -> float:
     return lib().orc_icdf_as26(p)
 
@@ -228,9 +234,10 @@ class Universe:
                 x[i] = float(v)
         return x
 
-    def _cfg(self, scheme, rng, scramble, semantics, seed, n_per_rep, sobol_dims_needed):
+    def _cfg(self, scheme, rng, scramble, semantics, seed, n_per_rep, sobol_dims_needed, icdf=0):
         cfg = _Cfg()
         cfg.scheme, cfg.rng, cfg.scramble, cfg.semantics = scheme, rng, scramble, semantics
+        cfg.icdf = icdf
         cfg.seed = seed & (2**64 - 1)
         cfg.n_paths_per_replicate = n_per_rep
         self._keep = None
@@ -243,13 +250,13 @@ class Universe:
 
     def simulate(self, times, initial_values, path_begin, path_end, *, scheme=EULER, rng=PSEUDO,
                  scramble=SHIFT, semantics=REFERENCE, seed=0, n_per_replicate=0, full=True,
-                 threads=1):
+                 threads=1, icdf=0):
         times = np.ascontiguousarray(times, dtype=np.float64)
         T, P = len(times), self.n_processes
         n = path_end - path_begin
         x0 = self.x0(initial_values)
         cfg = self._cfg(scheme, rng, scramble, semantics, seed, n_per_replicate or n,
-                        (T - 1) * self.n_stochastic)
+                        (T - 1) * self.n_stochastic, icdf)
         full_arr = np.zeros((n, T, P), dtype=np.float64) if full else None
         term = np.zeros((n, P), dtype=np.float64)
         err = C.create_string_buffer(1024)
@@ -263,13 +270,13 @@ class Universe:
 
     def estimate(self, times, initial_values, path_begin, path_end, payoff, *, scheme=EULER,
                  rng=PSEUDO, scramble=SHIFT, semantics=REFERENCE, seed=0, n_per_replicate=0,
-                 threads=1):
+                 threads=1, icdf=0):
         times = np.ascontiguousarray(times, dtype=np.float64)
         T = len(times)
         x0 = self.x0(initial_values)
         n = path_end - path_begin
         cfg = self._cfg(scheme, rng, scramble, semantics, seed, n_per_replicate or n,
-                        (T - 1) * self.n_stochastic)
+                        (T - 1) * self.n_stochastic, icdf)
         s, q = C.c_double(), C.c_double()
         err = C.create_string_buffer(1024)
         rc = lib().orc_estimate(self._h, times.ctypes.data_as(C.POINTER(C.c_double)), T,

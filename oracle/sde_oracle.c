@@ -847,6 +847,22 @@ double orc_icdf_as26(double p) {
     return p < 0.5 ? -x : x;
 }
 
+/* The "accurate" option (not in the reference): AS 26.2.23 refined by two
+ * Halley steps on Phi(z) - p, the residual formed from the tail probability
+ * through erfc.  Same algorithm as the engine's FP64 kernels. */
+double orc_icdf_accurate(double p) {
+    double z = orc_icdf_as26(p);
+    int lower = p < 0.5;
+    double tail = lower ? p : 1.0 - p;
+    for (int it = 0; it < 2; ++it) {
+        double ft = 0.5 * erfc((lower ? -z : z) * 0.70710678118654752);
+        double r = lower ? ft - tail : tail - ft;
+        double u = r * 2.5066282746310002 * exp(0.5 * z * z);
+        z = z - u / (1.0 + 0.5 * z * u);
+    }
+    return z;
+}
+
 uint64_t orc_poisson(double u, double lambda) {
     if (lambda <= 0.0) return 0;
     double p = exp(-lambda);
@@ -949,7 +965,7 @@ static double inc_sample(scen_t* s, const inc_t* inc, int tidx) {
     case INC_DT: return s->dts[tidx];
     case INC_DW: {
         double q = rng_sample(s, tidx, inc->idx);
-        return s->sqrt_dts[tidx] * orc_icdf_as26(q);
+        return s->sqrt_dts[tidx] * (s->cfg->icdf ? orc_icdf_accurate(q) : orc_icdf_as26(q));
     }
     default: {
         double uu = rng_sample(s, tidx, inc->idx);

@@ -54,6 +54,7 @@ typedef struct orc_cfg {
     uint64_t n_paths_per_replicate; /* N: XOR replicates restart points at 0 */
     const uint32_t* sobol_v;        /* [dims][32] direction numbers          */
     int sobol_dims;
+    int icdf;       /* 0: AS 26.2.23 (reference); 1: the accurate option      */
 } orc_cfg;
 
 /* ---- universe (equation parsing, src/proc/util.rs:52-166) ------------- */
@@ -108,6 +109,7 @@ void orc_sobol_points(const uint32_t* V, int dims, uint64_t first, uint64_t n,
 
 /* ---- inverse CDFs (src/proc/increment.rs:161-200) ---------------------- */
 double   orc_icdf_as26(double p);
+double   orc_icdf_accurate(double p);
 uint64_t orc_poisson(double u, double lambda);
 
 #ifdef __cplusplus

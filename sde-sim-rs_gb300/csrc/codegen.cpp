@@ -180,7 +180,7 @@ struct Gen {
     // the FP32 XOR path goes straight from the scrambled word to a normal;
     // q / up / gt are formed only where a jump count or RK's sign needs them
     bool needs_tail(int k) const {
-        return u.token_kind[k] == IncKind::Dn || (sp.scheme == SCHEME_RK && k == 0);
+        return u.token_kind[k] == IncKind::Dn || (sp.scheme == SCHEME_RK && k == 0) || sp.icdf != 0;
     }
     bool uses_chacha() const { return NI > 0 && !xorm(); }
     bool has_alg() const { return !u.alg.empty(); }
@@ -190,18 +190,28 @@ struct Gen {
     // blocks in registers (indices known at compile time).
     void uniform_from(Out& o, int k) const {
         const std::string K = S(k);
+        // FP32: the 53-bit uniform U (p = U 2^-53); the tail q / up / gt
+        // only where a jump count, RK's sign or the accurate icdf reads it
+        auto tail53 = [&]() {
+            if (needs_tail(k))
+                o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_u53(" + V("U", k) +
+                    ", " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
+        };
         if (sp.rng == RNG_PSEUDO) {
-            if (!f32) o.l("const double " + V("u", k) + " = sde_u64_to_f64(" + V("r", k) + ");");
-            else o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_u53(" +
-                     V("r", k) + " >> 11, " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
+            if (!f32) {
+                o.l("const double " + V("u", k) + " = sde_u64_to_f64(" + V("r", k) + ");");
+            } else {
+                o.l("const sde_u64 " + V("U", k) + " = " + V("r", k) + " >> 11;");
+                tail53();
+            }
         } else if (shiftm()) {
             o.l("const sde_u32 " + V("x", k) + " = sde_sobol_direct(a.sobol_v, t * " + S(NI) + " + " + K + ", " + V("G") + ");");
             if (!f32) {
                 o.l("const double " + V("v", k) + " = (double)" + V("x", k) + " * 0x1p-32 + sde_u64_to_f64(" + V("r", k) + ");");
                 o.l("const double " + V("u", k) + " = " + V("v", k) + " - trunc(" + V("v", k) + ");");
             } else {
-                o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_u53(sde_shift_u53(" +
-                    V("x", k) + ", " + V("r", k) + "), " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
+                o.l("const sde_u64 " + V("U", k) + " = sde_shift_u53(" + V("x", k) + ", " + V("r", k) + ");");
+                tail53();
             }
         } else {
             o.l("const int " + V("d", k) + " = t * " + S(NI) + " + " + K + ";");
@@ -262,11 +272,19 @@ struct Gen {
 
     // Wiener increments w<k> = sqrt_dt * icdf(u<k>)   (increment.rs:89-97)
     void wiener(Out& o, bool from_words = false) const {
+        const bool acc = sp.icdf != 0;
         for (int k = 0; k < NI; ++k) {
             if (u.token_kind[k] != IncKind::Dw) continue;
-            if (!f32) o.l("const double " + V("w", k) + " = sdt * sde_icdf_as26(" + V("u", k) + ");");
-            else if (from_words) o.l("const float " + V("w", k) + " = sdt * sde_normal_xor(" + V("y", k) + ");");
-            else o.l("const float " + V("w", k) + " = sdt * sde_icdf_as26_q(" + V("q", k) + ", " + V("up", k) + ");");
+            if (!f32)
+                o.l("const double " + V("w", k) + " = sdt * " + (acc ? "sde_icdf_accurate(" : "sde_icdf_as26(") +
+                    V("u", k) + ");");
+            else if (from_words && !acc)
+                o.l("const float " + V("w", k) + " = sdt * sde_normal_xor(" + V("y", k) + ");");
+            else if (!xorm() && !acc)
+                o.l("const float " + V("w", k) + " = sdt * sde_normal_u53(" + V("U", k) + ");");
+            else
+                o.l("const float " + V("w", k) + " = sdt * " + (acc ? "sde_icdf_accurate_q(" : "sde_icdf_as26_q(") +
+                    V("q", k) + ", " + V("up", k) + ");");
         }
     }
 
@@ -762,6 +780,7 @@ std::string emit_expression(const ExprP& e, bool fp32) {
 static std::string tag(const KernelSpec& s) {
     std::string r = s.scheme == SCHEME_RK ? "rk" : "euler";
     r += s.precision == PREC_FP32 ? "_fp32" : "_fp64";
+    if (s.icdf) r += "_acc";
     r += s.rng == RNG_PSEUDO ? "_pseudo" : (s.scramble == SCRAMBLE_XOR ? "_sobolxor" : "_sobolshift");
     if (s.ppt > 1) r += "_ppt" + std::to_string(s.ppt);
     return r;

@@ -24,6 +24,7 @@ struct KernelSpec {
     std::vector<ExprP> payoffs;         // resolved estimator expressions
     int block = 256;
     int ppt = 1;                        // paths per thread (independent chains)
+    int icdf = 0;                       // 0: AS 26.2.23 (reference), 1: accurate
     // adjoint: parameters and initial values to differentiate
     bool adjoint = false;
     std::vector<int> grad_params;       // parameter indices

@@ -167,16 +167,31 @@ SDE_DEV float sde_rcp_approx(float x) {
  * before its one rounding, log2 q = lg2(2m+1) - 33 folds into one FMA with
  * -2 ln 2, sqrt(a) = a * rsqrt(a) (a >= 2 ln 2 > 0), the rational term is
  * one reciprocal, and the sign (negative for p < 0.5) is one xor. */
+/* |z| of AS 26.2.23 from a = -2 ln q > 0 */
+SDE_DEV float sde_as26_abs(float a) {
+    const float t = a * sde_rsqrt_approx(a);
+    const float num = fmaf(fmaf(0.010328f, t, 0.802853f), t, 2.515517f);
+    const float den = fmaf(fmaf(fmaf(0.001308f, t, 0.189269f), t, 1.432788f), t, 1.0f);
+    return fmaf(-num, sde_rcp_approx(den), t);
+}
+
 SDE_DEV float sde_normal_xor(sde_u32 y) {
     const sde_u32 s = (sde_u32)((int)y >> 31);  /* all ones when p >= 0.5 */
     const sde_u32 m = y ^ s;                    /* min(y, ~y) */
     const float lg = sde_lg2_approx(__uint2float_rn(2u * m + 1u));
-    const float a = fmaf(lg, -1.3862943611198906f, 45.747713916956393f);  /* -2 ln q */
-    const float t = a * sde_rsqrt_approx(a);
-    const float num = fmaf(fmaf(0.010328f, t, 0.802853f), t, 2.515517f);
-    const float den = fmaf(fmaf(fmaf(0.001308f, t, 0.189269f), t, 1.432788f), t, 1.0f);
-    const float x = fmaf(-num, sde_rcp_approx(den), t);
+    const float x = sde_as26_abs(fmaf(lg, -1.3862943611198906f, 45.747713916956393f));  /* -2 ln q */
     return __int_as_float(__float_as_int(x) ^ (~s & 0x80000000u));
+}
+
+/* The same from a 53-bit uniform p = U 2^-53 (ChaCha doubles, or the
+ * reference's shifted Sobol values through sde_shift_u53): q = min(U,
+ * 2^53 - U) 2^-53, log2 q = lg2(Q) - 53. */
+SDE_DEV float sde_normal_u53(sde_u64 U) {
+    const bool up = U >= (1ull << 52);
+    const sde_u64 Q = up ? (1ull << 53) - U : U;
+    const float lg = sde_lg2_approx(__ull2float_rn(Q));
+    const float x = sde_as26_abs(fmaf(lg, -1.3862943611198906f, 73.473601139354201f));
+    return up ? x : -x;
 }
 
 /* The same rational approximation in FP32, from the exact tail q. */
@@ -186,6 +201,33 @@ SDE_DEV float sde_icdf_as26_q(float q, bool up) {
     const float den = ((0.001308f * t + 0.189269f) * t + 1.432788f) * t + 1.0f;
     const float x = t - __fdividef(num, den);
     return up ? x : -x;
+}
+
+/* "accurate" inverse normal (an option beside the reference's formula):
+ * the AS 26.2.23 value refined by Halley steps on Phi(z) - p, with the
+ * residual formed from the tail probability through erfc, so nothing
+ * cancels in the tails:  u = r / phi(z),  z <- z - u / (1 + z u / 2).
+ * FP64: two steps (|error| ~ 1e-16 from 4.5e-4); FP32: one step. */
+SDE_DEV double sde_icdf_accurate(double p) {
+    double z = sde_icdf_as26(p);
+    const bool lower = p < 0.5;
+    const double tail = lower ? p : 1.0 - p;
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const double ft = 0.5 * erfc((lower ? -z : z) * 0.70710678118654752);
+        const double r = lower ? ft - tail : tail - ft;
+        const double u = r * 2.5066282746310002 * exp(0.5 * z * z);
+        z = z - u / (1.0 + 0.5 * z * u);
+    }
+    return z;
+}
+
+SDE_DEV float sde_icdf_accurate_q(float q, bool up) {
+    float z = sde_icdf_as26_q(q, up);
+    const float ft = 0.5f * erfcf((up ? z : -z) * 0.70710678f);
+    const float r = up ? q - ft : ft - q;
+    const float u = r * 2.50662827f * expf(0.5f * z * z);
+    return z - u / (1.0f + 0.5f * z * u);
 }
 
 /* Poisson inverse CDF with the reference's cap of 200 (increment.rs:182-200) */

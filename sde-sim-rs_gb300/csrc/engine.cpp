@@ -378,6 +378,8 @@ static KernelSpec spec_from(const sde_options* o) {
     if (s.block % 32 != 0 || s.block > 1024) fail(SDE_ERR_INVALID, "block_size must be a multiple of 32 up to 1024");
     s.ckpt_every = o->ckpt_every > 0 ? o->ckpt_every : 19;
     s.ppt = o->paths_per_thread > 0 ? o->paths_per_thread : 1;
+    s.icdf = o->icdf;
+    if (s.icdf != SDE_ICDF_AS26 && s.icdf != SDE_ICDF_ACCURATE) fail(SDE_ERR_INVALID, "unknown icdf");
     if (s.ppt != 1 && s.ppt != 2 && s.ppt != 4) fail(SDE_ERR_INVALID, "paths_per_thread must be 1, 2 or 4");
     if (s.ckpt_every > 256) fail(SDE_ERR_INVALID, "ckpt_every must be at most 256");
     return s;

@@ -152,7 +152,8 @@ class Plan:
                  payoffs: Sequence[str] = (), scheme: str = "euler", rng: str = "pseudo",
                  scramble: str = "shift", precision: str = "fp64", semantics: str = "reference",
                  output: str = "full", block_size: int = 0, grad_params: Sequence[str] | None = None,
-                 grad_x0: Sequence[str] | None = None, ckpt_every: int = 0):
+                 grad_x0: Sequence[str] | None = None, ckpt_every: int = 0, paths_per_thread: int = 1,
+                 icdf: str = "as26"):
         """grad_params / grad_x0 make an adjoint plan: each run also returns
         the pathwise derivatives of E[payoffs[0]] with respect to those
         parameters and initial values (Euler-Maruyama, checkpoints every
@@ -169,6 +170,8 @@ class Plan:
         opts.output = N.OUTPUT[output]
         opts.block_size = block_size
         opts.ckpt_every = ckpt_every
+        opts.paths_per_thread = paths_per_thread
+        opts.icdf = N.ICDF[icdf]
         self.equations = list(equations)
         self.params = list(params)
         self.payoffs = list(payoffs)

@@ -27,6 +27,7 @@ SCRAMBLE = {"shift": 0, "xor": 1}
 PRECISION = {"fp64": 0, "fp32": 1}
 SEMANTICS = {"reference": 0, "textbook": 1}
 OUTPUT = {"full": 0, "checkpoints": 1, "terminal": 2, "none": 3}
+ICDF = {"as26": 0, "reference": 0, "accurate": 1}
 LAYOUT_REFERENCE, LAYOUT_DEVICE = 0, 1
 
 
@@ -34,7 +35,7 @@ class Options(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("scheme", C.c_int32), ("rng", C.c_int32),
                 ("scramble", C.c_int32), ("precision", C.c_int32), ("semantics", C.c_int32),
                 ("output", C.c_int32), ("block_size", C.c_int32), ("ckpt_every", C.c_int32),
-                ("paths_per_thread", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("paths_per_thread", C.c_int32), ("icdf", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class RunArgs(C.Structure):

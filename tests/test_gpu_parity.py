@@ -287,3 +287,21 @@ def test_caller_owned_device_buffer(engine):
     assert np.array_equal(buf.cpu().numpy().reshape(9, 2, 128), ref.astype(np.float32))
     with pytest.raises(ValueError, match="smaller than the filtration"):
         plan.run(times, {"S": 100.0, "v": 0.04}, 128, device_out=buf.data_ptr(), device_out_bytes=16)
+
+
+@pytest.mark.parametrize("rng", list(RNGS))
+def test_accurate_icdf_option(engine, oracle, rng):
+    times = np.linspace(0.0, 1.0, 33)
+    r, s = RNGS[rng]
+    eqs, init = CASES["heston"]
+    p64 = engine.Plan(eqs, rng=r, scramble=s, precision="fp64", icdf="accurate")
+    gpu = p64.run(times, init, 300, seed=5).values("reference")[0]
+    ref = oracle.Universe(eqs).simulate(times, init, 0, 300, seed=5, n_per_replicate=300, icdf=1,
+                                        **_oracle_cfg(oracle, "euler", rng, "reference"))
+    assert close64(gpu, ref)[1] == 0
+    p32 = engine.Plan(eqs, rng=r, scramble=s, precision="fp32", icdf="accurate", output="terminal")
+    g32 = p32.run(times, init, 2000, seed=5).values("reference")[0, :, 0, :]
+    r32 = oracle.Universe(eqs).simulate(times, init, 0, 2000, seed=5, n_per_replicate=2000, icdf=1, full=False,
+                                        **_oracle_cfg(oracle, "euler", rng, "reference"))
+    rel = np.abs(g32 - r32) / np.maximum(np.abs(r32), 1.0)
+    assert np.mean(rel < 1e-3) > 0.99

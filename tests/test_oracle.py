@@ -160,3 +160,11 @@ def test_missing_initial_value_is_zero(oracle):
     f = u.simulate([0.0, 1.0, 2.0], {"X": 1.0, "nope": 5.0}, 0, 1)
     assert f[0, 0].tolist() == [1.0, 0.0]
     assert f[0, 2].tolist() == [3.0, 3.0]
+
+
+def test_icdf_accurate_option(oracle):
+    sp = pytest.importorskip("scipy.special")
+    p = np.concatenate([np.logspace(-300, -1, 60), np.linspace(0.01, 0.99, 99), 1 - np.logspace(-16, -1, 30)])
+    got = np.array([oracle.icdf_accurate(float(x)) for x in p])
+    want = sp.ndtri(p)
+    assert np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0)) < 2e-15
