@@ -1202,6 +1202,8 @@ static void* run_job(void* arg) {
     double* vb = (double*)calloc(P > 0 ? P : 1, sizeof(double));
     double* vc = (double*)calloc(P > 0 ? P : 1, sizeof(double));
     double* prow = (double*)calloc(s.nslots, sizeof(double));
+    uint32_t* masks = (uint32_t*)calloc(ndims > 0 ? ndims : 1, sizeof(uint32_t));
+    uint64_t mask_rep = UINT64_MAX;
 
     for (uint64_t sc = J->begin; sc < J->end && !s.err; ++sc) {
         /* ScenarioFiltration::new (src/filtration.rs:22-53) */
@@ -1228,13 +1230,18 @@ static void* run_job(void* arg) {
                     s.sobol_vals[d] = v - trunc(v);
                 }
             } else {
+                /* XOR masks of replicate r (high words of ChaCha8(seed + r)),
+                 * made once per replicate and thread */
                 uint64_t N = cfg->n_paths_per_replicate ? cfg->n_paths_per_replicate : 1;
                 uint64_t r = sc / N, n = sc % N;
-                chacha_stream ms;
-                cs_init(&ms, cfg->seed + r);
+                if (r != mask_rep) {
+                    chacha_stream ms;
+                    cs_init(&ms, cfg->seed + r);
+                    for (size_t d = 0; d < ndims; ++d) masks[d] = (uint32_t)(cs_next_u64(&ms) >> 32);
+                    mask_rep = r;
+                }
                 for (size_t d = 0; d < ndims; ++d) {
-                    uint32_t m = (uint32_t)(cs_next_u64(&ms) >> 32);
-                    uint32_t y = sobol_point(cfg->sobol_v, (int)d, n) ^ m;
+                    uint32_t y = sobol_point(cfg->sobol_v, (int)d, n) ^ masks[d];
                     s.sobol_vals[d] = ((double)y + 0.5) * (1.0 / 4294967296.0);
                 }
             }
@@ -1263,7 +1270,7 @@ static void* run_job(void* arg) {
     }
     J->err = s.err;
     free(s.dts); free(s.sqrt_dts); free(s.raw); free(s.slots); free(s.step_vals);
-    free(s.sobol_vals); free(incs); free(va); free(vb); free(vc); free(prow);
+    free(s.sobol_vals); free(incs); free(va); free(vb); free(vc); free(prow); free(masks);
     return NULL;
 }
 

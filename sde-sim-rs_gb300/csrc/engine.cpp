@@ -310,6 +310,7 @@ struct sde_plan {
     sde::Universe u;
     sde::KernelSpec spec;
     int output = SDE_OUT_FULL;
+    bool auto_block = true;  // block size chosen per run from the path count
     std::string source;
     std::string fwd_name, adj_name;
     std::shared_ptr<sde::Cubin> cubin;
@@ -393,6 +394,7 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
     p->u = parse_universe(eqs, params);
     p->spec = spec_from(&o);
     p->output = o.output;
+    p->auto_block = o.block_size <= 0;
     for (const auto& s : payoffs) p->spec.payoffs.push_back(p->u.resolve(parse_expression(s)));
     if (grad_params || grad_x0) {
         if (p->spec.payoffs.empty()) fail(SDE_ERR_INVALID, "an adjoint plan needs a payoff");
@@ -443,9 +445,19 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     if (sobol && !xorm && a.path_offset + total + 5 > (1ull << 32))
         fail(SDE_ERR_UNSUPPORTED, "Sobol point index beyond 2^32");
     if (xorm && N > (1ull << 32)) fail(SDE_ERR_UNSUPPORTED, "more than 2^32 Sobol points per replicate");
-    const int block = p->spec.block;
     // the adjoint kernel steps one path per thread
-    const uint64_t per_block = (uint64_t)block * (p->spec.adjoint ? 1 : p->spec.ppt);
+    const int ppt_eff = p->spec.adjoint ? 1 : p->spec.ppt;
+    int block = p->spec.block;
+    if (p->auto_block) {
+        // few paths (the reference's 10,000): spread the warps over every SM
+        // rather than filling a few with 8-warp blocks
+        int dev = 0, sms = 148;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const uint64_t warps = (N + 32ull * ppt_eff - 1) / (32ull * ppt_eff) * (uint64_t)a.n_replicates;
+        const uint64_t wpb = std::min<uint64_t>(8, std::max<uint64_t>(1, (warps + sms - 1) / std::max(1, sms)));
+        block = (int)(32 * wpb);
+    }
+    const uint64_t per_block = (uint64_t)block * ppt_eff;
     const uint64_t gx = (N + per_block - 1) / per_block;
     if (gx > 0x7fffffffull) fail(SDE_ERR_INVALID, "too many paths for one launch");
 

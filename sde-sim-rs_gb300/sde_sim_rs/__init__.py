@@ -114,7 +114,6 @@ class Result:
         """The reference's long/tidy frame: polars if importable, else pyarrow,
         else a Frame of numpy columns."""
         cols = self.long()
-        names = np.asarray(self.process_names, dtype=object)
         if fmt in ("auto", "polars"):
             try:
                 import polars as pl  # noqa: F401
@@ -130,8 +129,9 @@ class Result:
             except ImportError:
                 if fmt == "arrow":
                     raise
-        return Frame(scenario=cols["scenario"], time=cols["time"],
-                     process_name=names[cols["process"]] if len(names) else cols["process"],
+        # fixed-width unicode gather: no per-row Python objects
+        ustr = np.asarray(list(self.process_names) or [""], dtype=str)
+        return Frame(scenario=cols["scenario"], time=cols["time"], process_name=ustr[cols["process"]],
                      value=cols["value"])
 
 
