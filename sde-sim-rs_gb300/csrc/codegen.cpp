@@ -273,8 +273,28 @@ struct Gen {
     // Wiener increments w<k> = sqrt_dt * icdf(u<k>)   (increment.rs:89-97)
     void wiener(Out& o, bool from_words = false) const {
         const bool acc = sp.icdf != 0;
+        // FP32 with the AS 26.2.23 normal: pairs of Wiener indices share
+        // paired FP32 arithmetic (fma.f32x2)
+        std::vector<int> paired;
+        if (f32 && !acc && (from_words || !xorm())) {
+            std::vector<int> ks;
+            for (int k = 0; k < NI; ++k)
+                if (u.token_kind[k] == IncKind::Dw) ks.push_back(k);
+            for (size_t i = 0; i + 1 < ks.size(); i += 2) {
+                const int ka = ks[i], kb = ks[i + 1];
+                const std::string pr = V("wp" + S(ka) + "_", kb);
+                const std::string src = xorm() ? "sde_normal_xor2(" + V("y", ka) + ", " + V("y", kb) + ")"
+                                                : "sde_normal_u53_2(" + V("U", ka) + ", " + V("U", kb) + ")";
+                o.l("const float2 " + pr + " = __fmul2_rn(make_float2(sdt, sdt), " + src + ");");
+                o.l("const float " + V("w", ka) + " = " + pr + ".x;");
+                o.l("const float " + V("w", kb) + " = " + pr + ".y;");
+                paired.push_back(ka);
+                paired.push_back(kb);
+            }
+        }
         for (int k = 0; k < NI; ++k) {
             if (u.token_kind[k] != IncKind::Dw) continue;
+            if (std::find(paired.begin(), paired.end(), k) != paired.end()) continue;
             if (!f32)
                 o.l("const double " + V("w", k) + " = sdt * " + (acc ? "sde_icdf_accurate(" : "sde_icdf_as26(") +
                     V("u", k) + ");");

@@ -183,6 +183,43 @@ SDE_DEV float sde_normal_xor(sde_u32 y) {
     return __int_as_float(__float_as_int(x) ^ (~s & 0x80000000u));
 }
 
+/* Two normals at once: the polynomial and scaling work of both runs as
+ * paired FP32 operations (one fma.f32x2 per pair of FMAs); the SFU work
+ * (lg2, rsqrt, rcp) stays per element.  The numerator is formed negated so
+ * the final step is a plain paired FMA. */
+SDE_DEV float2 sde_as26_abs2(float2 a) {
+    const float2 r = make_float2(sde_rsqrt_approx(a.x), sde_rsqrt_approx(a.y));
+    const float2 t = __fmul2_rn(a, r);
+    const float2 nnum = __ffma2_rn(__ffma2_rn(make_float2(-0.010328f, -0.010328f), t,
+                                              make_float2(-0.802853f, -0.802853f)),
+                                   t, make_float2(-2.515517f, -2.515517f));
+    const float2 den = __ffma2_rn(__ffma2_rn(__ffma2_rn(make_float2(0.001308f, 0.001308f), t,
+                                                        make_float2(0.189269f, 0.189269f)),
+                                             t, make_float2(1.432788f, 1.432788f)),
+                                  t, make_float2(1.0f, 1.0f));
+    const float2 rc = make_float2(sde_rcp_approx(den.x), sde_rcp_approx(den.y));
+    return __ffma2_rn(nnum, rc, t);
+}
+
+SDE_DEV float2 sde_normal_xor2(sde_u32 ya, sde_u32 yb) {
+    const sde_u32 sa = (sde_u32)((int)ya >> 31), sb = (sde_u32)((int)yb >> 31);
+    const float2 lg = make_float2(sde_lg2_approx(__uint2float_rn(2u * (ya ^ sa) + 1u)),
+                                  sde_lg2_approx(__uint2float_rn(2u * (yb ^ sb) + 1u)));
+    const float2 x = sde_as26_abs2(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
+                                              make_float2(45.747713916956393f, 45.747713916956393f)));
+    return make_float2(__int_as_float(__float_as_int(x.x) ^ (~sa & 0x80000000u)),
+                       __int_as_float(__float_as_int(x.y) ^ (~sb & 0x80000000u)));
+}
+
+SDE_DEV float2 sde_normal_u53_2(sde_u64 Ua, sde_u64 Ub) {
+    const bool upa = Ua >= (1ull << 52), upb = Ub >= (1ull << 52);
+    const sde_u64 Qa = upa ? (1ull << 53) - Ua : Ua, Qb = upb ? (1ull << 53) - Ub : Ub;
+    const float2 lg = make_float2(sde_lg2_approx(__ull2float_rn(Qa)), sde_lg2_approx(__ull2float_rn(Qb)));
+    const float2 x = sde_as26_abs2(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
+                                              make_float2(73.473601139354201f, 73.473601139354201f)));
+    return make_float2(upa ? x.x : -x.x, upb ? x.y : -x.y);
+}
+
 /* The same from a 53-bit uniform p = U 2^-53 (ChaCha doubles, or the
  * reference's shifted Sobol values through sde_shift_u53): q = min(U,
  * 2^53 - U) 2^-53, log2 q = lg2(Q) - 53. */

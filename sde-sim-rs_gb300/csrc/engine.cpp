@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
+#include <list>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -664,6 +665,9 @@ void sde_run_args_init(sde_run_args* a) {
     a->n_replicates = 1;
 }
 
+static std::mutex g_sim_mu;
+static std::list<std::pair<std::string, std::shared_ptr<sde_plan>>> g_sim_plans;  // most recent first
+
 static std::vector<std::string> strs(const char* const* s, int n) {
     std::vector<std::string> v;
     for (int i = 0; i < n; ++i) {
@@ -811,7 +815,27 @@ int sde_simulate(const char* const* equations, int32_t n_equations, const double
         else if (std::strcmp(scheme, "runge-kutta") == 0) o.scheme = SDE_SCHEME_RK;
         else fail(SDE_ERR_INVALID, std::string("unknown scheme '") + scheme + "'");
         o.rng = std::strcmp(rng_method, "sobol") == 0 ? SDE_RNG_SOBOL : SDE_RNG_PSEUDO;
-        std::shared_ptr<sde_plan> plan(plan_create(strs(equations, n_equations), {}, {}, o));
+        // the one-shot entry keeps recently lowered universes: repeated calls
+        // with the same equations skip parsing, lowering and module loading
+        const auto eqs = strs(equations, n_equations);
+        std::string key = std::to_string(o.scheme) + "|" + std::to_string(o.rng);
+        for (const auto& e : eqs) key += "\x1f" + e;
+        std::shared_ptr<sde_plan> plan;
+        {
+            std::lock_guard<std::mutex> g(g_sim_mu);
+            for (auto it = g_sim_plans.begin(); it != g_sim_plans.end(); ++it)
+                if (it->first == key) {
+                    plan = it->second;
+                    g_sim_plans.splice(g_sim_plans.begin(), g_sim_plans, it);
+                    break;
+                }
+        }
+        if (!plan) {
+            plan.reset(plan_create(eqs, {}, {}, o));
+            std::lock_guard<std::mutex> g(g_sim_mu);
+            g_sim_plans.emplace_front(key, plan);
+            if (g_sim_plans.size() > 16) g_sim_plans.pop_back();
+        }
         std::vector<double> x0(std::max(1, plan->u.n_processes()), 0.0);
         for (int k = 0; k < n_init; ++k) {
             int idx = plan->u.process_index(init_names[k]);
