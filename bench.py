@@ -81,6 +81,29 @@ def basket_equations(dim: int = 64, seed: int = 2024):
     return eqs, payoff, sigma, L
 
 
+def combine_ranks(ms_step: float, rep_means, world: int):
+    """Weak-scaled replicas across ranks: the job's step time is the slowest
+    rank's, and the replicate means of all ranks (disjoint replicate seeds)
+    form one RQMC estimate.  Returns (ms_step, estimate, se, n_replicates).
+    Works with any initialised torch.distributed backend (NCCL on the GPUs,
+    gloo in the CPU test)."""
+    import torch
+    import torch.distributed as dist
+    means = torch.as_tensor(rep_means, dtype=torch.float64).reshape(-1)
+    if world > 1:
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([ms_step], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+        parts = [torch.zeros_like(means, device=dev) for _ in range(world)]
+        dist.all_gather(parts, means.to(dev))
+        means = torch.cat([p.cpu() for p in parts])
+    n = means.numel()
+    est = float(means.mean())
+    se = float(means.std(unbiased=True) / math.sqrt(n)) if n > 1 else float("nan")
+    return ms_step, est, se, n
+
+
 def dist_init(n_gpus):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -226,17 +249,10 @@ def run_engine(args):
     if world > 1:
         torch.distributed.barrier()
     ms = [a.elapsed_time(b) for a, b in ev]
-    ms_step = sum(ms) / len(ms)
-    if world > 1:
-        t = torch.tensor([ms_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
+    sums = results[-1].estimates()[0][:, 0]
+    ms_step, price, price_se, _ = combine_ranks(sum(ms) / len(ms), sums / npaths, world)
     path_steps = npaths * reps * STEPS_T
     value = path_steps * world / (ms_step * 1e-3)
-    sums = results[-1].estimates()[0][:, 0]
-    rep_means = sums / npaths
-    price = float(rep_means.mean())
-    price_se = float(rep_means.std(ddof=1) / math.sqrt(reps))
 
     # end to end through the public API: pinned H2D of the step's inputs,
     # kernel, D2H of the estimates, every step (host wall clock)

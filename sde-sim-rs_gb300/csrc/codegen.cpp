@@ -275,8 +275,10 @@ struct Gen {
         const bool acc = sp.icdf != 0;
         // FP32 with the AS 26.2.23 normal: pairs of Wiener indices share
         // paired FP32 arithmetic (fma.f32x2)
+        // (wide universes -- dozens of normals per step feeding long FMA
+        // chains -- are register-bound already; pairing is kept to <= 16)
         std::vector<int> paired;
-        if (f32 && !acc && (from_words || !xorm())) {
+        if (f32 && !acc && (from_words || !xorm()) && NI <= 16) {
             std::vector<int> ks;
             for (int k = 0; k < NI; ++k)
                 if (u.token_kind[k] == IncKind::Dw) ks.push_back(k);
