@@ -200,6 +200,24 @@ int sde_result_copy_long(sde_result* r, int32_t* scenario, double* time,
  * [n_replicates][sde_plan_n_estimates].                                   */
 int sde_result_estimates(sde_result* r, double* host_sum, double* host_sumsq);
 
+/* ---- estimates with no device allocation --------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (their device memory comes from an arena or budget they do not
+ * control, or an allocation's implicit synchronisation is not acceptable
+ * where they call): runs a forward, pseudo-random plan and returns its
+ * estimator sums with every piece of scratch in one 4 MiB static device
+ * array of the library (held by each GPU that loads it until exit).  Host
+ * inputs; host outputs host_sum / host_sumsq [n_replicates][n_payoffs];
+ * synchronous on stream.  A run needing more than 4 MiB of scratch (about
+ * 5e5 blocks x payoffs x replicates) fails with SDE_ERR_INVALID.  The
+ * first call on a device loads the plan's kernels and resolves the array's
+ * address; make it before any stream capture.  Every call shares the
+ * array: calls that overlap on the GPU (other streams, other threads) race. */
+int sde_run_estimates_static(sde_plan* plan, const double* times, int32_t n_times,
+                             const double* x0, int32_t n_x0, const double* params, int32_t n_params,
+                             uint64_t n_paths, int32_t n_replicates, uint64_t seed, void* stream,
+                             double* host_sum, double* host_sumsq);
+
 /* ---- batched instances ---------------------------------------------------
  * No counterpart in the reference (one universe per simulate call): many
  * independent instances of a few templates (plans from sde_plan_create,

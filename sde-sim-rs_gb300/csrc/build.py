@@ -105,12 +105,13 @@ def build(verbose: bool = False) -> str:
         if _stale(o, [s] + headers):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
                          *inc, "-c", s, "-o", o])
-    o = os.path.join(OBJ, "kernels.o")
-    objs.append(o)
-    s = os.path.join(HERE, "kernels.cu")
-    if _stale(o, [s] + headers):
-        jobs.append(["nvcc", ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     *inc, "-c", s, "-o", o])
+    for src in ("kernels.cu", "noalloc.cu"):
+        o = os.path.join(OBJ, src.replace(".cu", ".o"))
+        objs.append(o)
+        s = os.path.join(HERE, src)
+        if _stale(o, [s] + headers + [os.path.join(HERE, "engine_internal.h")]):
+            jobs.append(["nvcc", ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         *inc, "-c", s, "-o", o])
     procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
              for j in jobs]
     failed = []

@@ -30,6 +30,7 @@
 #include "_gen/joe_kuo_d6.h"
 #include "codegen.h"
 #include "frontend.h"
+#include "engine_internal.h"
 #include "kernels.h"
 
 namespace sde {
@@ -1011,6 +1012,29 @@ int sde_probe_sfu_peak(double* ops) {
 }
 
 }  // extern "C"
+
+namespace sde {
+
+int plan_view(sde_plan* p, PlanView* v) {
+    return guarded([&] {
+        if (!p || !v) fail(SDE_ERR_INVALID, "NULL argument");
+        Loaded& L = ensure_loaded(p);
+        v->kernel = (void*)L.fwd;
+        v->n_processes = p->u.n_processes();
+        v->n_stochastic = p->u.n_stochastic();
+        v->n_payoffs = (int)p->spec.payoffs.size();
+        v->n_params = (int)p->u.params.size();
+        v->block = p->spec.block;
+        v->ppt = p->spec.ppt;
+        v->rng = p->spec.rng;
+        v->scheme = p->spec.scheme;
+        v->adjoint = p->spec.adjoint ? 1 : 0;
+    });
+}
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+}  // namespace sde
 
 // ===========================================================================
 // Batched instances: one persistent work-queue kernel over many instances

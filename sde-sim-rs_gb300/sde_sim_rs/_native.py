@@ -99,6 +99,9 @@ SIGNATURES = {
     "sde_result_copy_values": ([C.c_void_p, C.c_void_p, C.c_int32], C.c_int),
     "sde_result_copy_long": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sde_result_estimates": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sde_run_estimates_static": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                  C.c_int32, C.c_uint64, C.c_int32, C.c_uint64, C.c_void_p, C.c_void_p,
+                                  C.c_void_p], C.c_int),
     "sde_batch_create": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)], C.c_int),
     "sde_batch_destroy": ([C.c_void_p], C.c_int),
     "sde_batch_prepare": ([C.c_void_p, C.POINTER(BatchInstances), C.c_int32, C.c_void_p,
