@@ -496,7 +496,7 @@ def run_batched(args):
     import torch
     import sde_sim_rs
     from sde_sim_rs.batch import Batch
-    tid, steps, paths, seeds, x0, params = batched_instances()
+    tid, steps, paths, seeds, x0, params = batched_instances(n=args.instances)
     tg = sde_sim_rs.Plan(GBM_P, params=["mu", "sigma"], payoffs=["X"], precision="fp32", output="none")
     to = sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], precision="fp32", output="none")
     stream = torch.cuda.current_stream()
@@ -535,7 +535,7 @@ def run_batched(args):
         se = math.sqrt(max(rq[0, 0] / N - m64 ** 2, 0) / N)
         z.append(abs(s[i, 0] / N - m64) / max(se, 1e-300))
     z = np.array(z)
-    _common(args, "batched_4096_gbm_ou_fp32", "path-steps/s (fwd, 4096 batched instances, FP32)",
+    _common(args, f"batched_{len(tid)}_gbm_ou_fp32", f"path-steps/s (fwd, {len(tid)} batched instances, FP32)",
             ps / (ms_step * 1e-3), ms_step, "f32", clk.summary(),
             {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
              "d2h_bytes_per_step": len(tid) * 16, "note": "graph replay + results read back"},
@@ -553,7 +553,8 @@ def run_adjoint(args):
     import numpy as np
     import torch
     import sde_sim_rs
-    n, T = 1 << 20, np.linspace(0.0, 1.0, 366)
+    n = args.paths if args.paths != N_PATHS else 1 << 20
+    T = np.linspace(0.0, 1.0, 366)
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     out = {}
@@ -597,6 +598,7 @@ def main():
     ap.add_argument("--paths", type=int, default=N_PATHS)
     ap.add_argument("--reps", type=int, default=REPS)
     ap.add_argument("--fp64-paths", type=int, default=1 << 14)
+    ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--workload", default="heston_rqmc",
                     choices=["heston_rqmc", "gbm_full", "basket", "batched", "adjoint"])

@@ -129,10 +129,13 @@ class Result:
             except ImportError:
                 if fmt == "arrow":
                     raise
-        # fixed-width unicode gather: no per-row Python objects
+        # rows cycle through the processes in order (src/filtration.rs:87-91),
+        # so the name column is the name list tiled: fixed-width unicode, no
+        # per-row Python objects and no gather
         ustr = np.asarray(list(self.process_names) or [""], dtype=str)
-        return Frame(scenario=cols["scenario"], time=cols["time"], process_name=ustr[cols["process"]],
-                     value=cols["value"])
+        P = max(1, self.n_processes)
+        names = np.tile(ustr[:P], len(cols["process"]) // P)
+        return Frame(scenario=cols["scenario"], time=cols["time"], process_name=names, value=cols["value"])
 
 
 def _arrow_table(cols, process_names, pa):
