@@ -413,10 +413,13 @@ def run_gbm_full(args):
     ms_step = sum(ms) / len(ms)
     ps = n * 252
     xt = res[-1].values("device")[0, -1, 0]
+    # the drop-in's first call lowers and loads the universe; later calls
+    # with the same equations reuse it
+    sde_sim_rs.simulate(GBM, T, n, {"X": 100.0}, "pseudo", "euler", seed=42, output_format="numpy")
     t0 = time.perf_counter()
-    for _ in range(3):
+    for _ in range(args.steps):
         fr = sde_sim_rs.simulate(GBM, T, n, {"X": 100.0}, "pseudo", "euler", seed=42, output_format="numpy")
-    e2e_s = (time.perf_counter() - t0) / 3
+    e2e_s = (time.perf_counter() - t0) / args.steps
     rows = len(fr["value"])
     nbytes = n * 253 * 8
     peak = _peaks()

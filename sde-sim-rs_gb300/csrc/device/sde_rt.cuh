@@ -326,6 +326,89 @@ template <class R> SDE_DEV R sde_logb(R b, R x) { return log(x) / log(b); }
 template <class R> SDE_DEV R sde_round2(R m, R x) { return round(x / m) * m; }
 
 /* ------------------------------------------------------------------------
+ * 5th-generation tensor cores (tcgen05) for correlated diffusions: the
+ * per-step increments d = K w of a universe whose diffusion terms are
+ * constant * own state are one [paths x dims] x [dims x processes] product.
+ * A (the paths' Wiener increments) and B (the constant matrix) sit in shared
+ * memory in the no-swizzle K-major core-matrix layout (8 rows x 16 bytes per
+ * core matrix, LBO = next core matrix along K, SBO = next 8-row group); the
+ * FP32 accumulator D lives in tensor memory and comes back one row (path)
+ * per thread with tcgen05.ld 32x32b.
+ * ---------------------------------------------------------------------- */
+
+SDE_DEV sde_u32 sde_smem_addr(const void* p) { return (sde_u32)__cvta_generic_to_shared(p); }
+
+/* matrix descriptor: start, LBO, SBO (bytes, >> 4), version 1, no swizzle */
+SDE_DEV sde_u64 sde_smem_desc(sde_u32 saddr, sde_u32 lbo, sde_u32 sbo) {
+    return (sde_u64)((saddr & 0x3FFFFu) >> 4) | ((sde_u64)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((sde_u64)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+/* instruction descriptor, kind::tf32: F32 accumulator, TF32 A and B, both
+ * K-major, N >> 3 at bit 17, M >> 4 at bit 24 */
+SDE_DEV sde_u32 sde_idesc_tf32(int M, int N) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((sde_u32)(N >> 3) << 17) | ((sde_u32)(M >> 4) << 24);
+}
+
+SDE_DEV void sde_tmem_alloc(sde_u32 dst_smem, sde_u32 ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+SDE_DEV void sde_tmem_dealloc(sde_u32 taddr, sde_u32 ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+SDE_DEV void sde_mbar_init(sde_u32 mbar, sde_u32 count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+SDE_DEV bool sde_mbar_try_wait(sde_u32 mbar, sde_u32 parity) {
+    sde_u32 ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+/* waits for the barrier phase, giving up after ~1 s of SM clock */
+SDE_DEV bool sde_mbar_wait_bounded(sde_u32 mbar, sde_u32 parity) {
+    const long long t0 = clock64();
+    while (!sde_mbar_try_wait(mbar, parity))
+        if (clock64() - t0 > 2000000000ll) return false;
+    return true;
+}
+SDE_DEV void sde_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+SDE_DEV void sde_tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+SDE_DEV void sde_tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+SDE_DEV void sde_mma_tf32(sde_u32 dtmem, sde_u64 adesc, sde_u64 bdesc, sde_u32 idesc, sde_u32 accumulate) {
+    asm volatile(
+        "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p; }" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+SDE_DEV void sde_mma_commit(sde_u32 mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+/* 16 consecutive FP32 columns of this thread's TMEM lane */
+SDE_DEV void sde_tmem_ld16(sde_u32 taddr, float* d) {
+    sde_u32 r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) d[i] = __uint_as_float(r[i]);
+}
+SDE_DEV void sde_tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+/* TF32 split x = hi + lo (hi keeps the 19 bits a TF32 operand reads) */
+SDE_DEV float sde_tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+/* ------------------------------------------------------------------------
  * Estimator reduction (fused epilogue): warp shuffles, then a Neumaier
  * compensated sum over the block's warps, in FP64.  out gets
  * {sum, compensation, sum of squares, compensation} per estimator.
