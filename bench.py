@@ -452,20 +452,30 @@ def run_basket(args):
     n = args.paths if args.paths != N_PATHS else 1 << 21
     T = [i / 128 for i in range(129)]
     ck = list(range(4, 129, 4))
-    plan = sde_sim_rs.Plan(eqs, payoffs=[payoff], rng="sobol", scramble="xor", precision="fp32",
-                           output="checkpoints")
+    init = {f"S{i + 1}": 100.0 for i in range(64)}
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    one = lambda: plan.run(T, {f"S{i + 1}": 100.0 for i in range(64)}, n, seed=7, checkpoints=ck, stream=stream)
-    for _ in range(args.warmup):
-        one().wait()
-    with Clocks(0) as clk:
-        ms, res = _timed_runs(one, args.steps, stream, flush)
-    ms_step = sum(ms) / len(ms)
-    s, q = res[-1].estimates()
-    price = s[0, 0] / n
-    se = math.sqrt(max(q[0, 0] / n - price ** 2, 0) / n)
-    del res
+    # the CUDA-core kernel (one FMA chain per process) and the tcgen05 one
+    # (the 64 x 64 diffusion product as 3xTF32 MMAs per 128 paths)
+    legs = {}
+    for leg, tc in (("cuda_cores", False), ("tensor_cores", True)):
+        if tc and args.cuda_cores_only:
+            continue
+        plan = sde_sim_rs.Plan(eqs, payoffs=[payoff], rng="sobol", scramble="xor", precision="fp32",
+                               output="checkpoints", tensor_cores=tc)
+        one = lambda plan=plan: plan.run(T, init, n, seed=7, checkpoints=ck, stream=stream)
+        for _ in range(args.warmup):
+            one().wait()
+        with Clocks(0) as clk:
+            ms, res = _timed_runs(one, args.steps, stream, flush)
+        s, q = res[-1].estimates()
+        del res
+        price = s[0, 0] / n
+        legs[leg] = {"plan": plan, "one": one, "clk": clk, "ms": sum(ms) / len(ms), "price": price,
+                     "se": math.sqrt(max(q[0, 0] / n - price ** 2, 0) / n), "tc": plan.uses_tensor_cores}
+    main_leg = legs.get("tensor_cores", legs["cuda_cores"])
+    one, clk, ms_step = main_leg["one"], main_leg["clk"], main_leg["ms"]
+    price, se = main_leg["price"], main_leg["se"]
     ps = n * 128
     nbytes = n * 64 * 32 * 4
     peak = _peaks()
@@ -489,7 +499,10 @@ def run_basket(args):
              "bytes_written_per_launch": nbytes},
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
              "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, estimator only"},
-            {"paths": n, "steps": 128, "checkpoints": 32, "price": price, "price_se": se})
+            {"paths": n, "steps": 128, "checkpoints": 32, "price": price, "price_se": se,
+             "kernel": "tcgen05 (3xTF32)" if main_leg["tc"] else "CUDA cores",
+             "legs": {k: {"ms": v["ms"], "path_steps_per_s": ps / (v["ms"] * 1e-3), "price": v["price"],
+                          "tensor_cores": v["tc"]} for k, v in legs.items()}})
 
 
 def run_batched(args):
@@ -603,6 +616,8 @@ def main():
     ap.add_argument("--fp64-paths", type=int, default=1 << 14)
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--cuda-cores-only", action="store_true",
+                    help="basket: time only the CUDA-core kernel (no tcgen05 leg)")
     ap.add_argument("--workload", default="heston_rqmc",
                     choices=["heston_rqmc", "gbm_full", "basket", "batched", "adjoint"])
     args = ap.parse_args()

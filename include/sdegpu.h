@@ -79,8 +79,19 @@ typedef struct sde_options {
     int32_t paths_per_thread; /* independent paths a thread steps in
                                lockstep (1, 2 or 4), 0 = 1                 */
     int32_t icdf;           /* SDE_ICDF_*          default AS26            */
-    int32_t reserved[5];
+    int32_t tensor_cores;   /* SDE_TC_*            default OFF             */
+    int32_t reserved[4];
 } sde_options;
+
+/* TC_ON: when the plan is FP32 Euler-Maruyama, forward, one path per
+ * thread, without algebraic processes, and every dW coefficient is a
+ * constant times its own process (correlated GBM baskets), the step's
+ * Wiener terms run as one tcgen05 TF32 product per 128 paths (3xTF32,
+ * about FP32 accuracy) and the block size is 128.  Other plans keep the
+ * CUDA-core kernel; sde_plan_tensor_cores tells which was built.
+ * No counterpart in the reference (its coefficient loop is
+ * src/sim/euler.rs:17-33).                                                */
+enum { SDE_TC_OFF = 0, SDE_TC_ON = 1 };
 
 /* AS26: the reference's Abramowitz-Stegun 26.2.23 normal (|err| ~ 4.5e-4).
  * ACCURATE: that value refined by Halley steps on Phi through erfc of the
@@ -157,6 +168,9 @@ int sde_plan_stochastic_token(const sde_plan* plan, int32_t i, char* buf, size_t
 int sde_plan_source(const sde_plan* plan, char* buf, size_t buf_len, size_t* needed);
 /* The NVRTC / ptxas log of the plan's compilation (registers, spills). */
 int sde_plan_compile_log(const sde_plan* plan, char* buf, size_t buf_len, size_t* needed);
+/* *on = 1 if the forward kernel was lowered to tcgen05 (SDE_TC_ON and an
+ * eligible universe), else 0.  No counterpart in the reference. */
+int sde_plan_tensor_cores(const sde_plan* plan, int32_t* on);
 
 /* ---- runs --------------------------------------------------------------
  * Replaces the scenario loop of sde_sim_rs::sim::simulate

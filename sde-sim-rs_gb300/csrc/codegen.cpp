@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <functional>
 #include <numeric>
 #include <sstream>
@@ -130,6 +131,63 @@ struct Out {
 };
 
 std::string S(int v) { return std::to_string(v); }
+
+// Value of an expression that reads no variable (plain f64 arithmetic, as
+// fasteval evaluates it); false if it reads one or uses an unfolded call.
+bool fold_const(const ExprP& e, double& v) {
+    double a = 0.0, b = 0.0;
+    switch (e->op) {
+    case Op::Const: v = e->value; return true;
+    case Op::Var: return false;
+    case Op::Neg: if (!fold_const(e->args[0], a)) return false; v = -a; return true;
+    case Op::Add: case Op::Sub: case Op::Mul: case Op::Div: case Op::Pow:
+        if (!fold_const(e->args[0], a) || !fold_const(e->args[1], b)) return false;
+        v = e->op == Op::Add ? a + b : e->op == Op::Sub ? a - b : e->op == Op::Mul ? a * b
+          : e->op == Op::Div ? a / b : std::pow(a, b);
+        return true;
+    case Op::Call:
+        if (e->args.size() != 1 || !fold_const(e->args[0], a)) return false;
+        if (e->fn == Fn::Sqrt) { v = std::sqrt(a); return true; }
+        if (e->fn == Fn::Exp) { v = std::exp(a); return true; }
+        if (e->fn == Fn::Abs) { v = std::fabs(a); return true; }
+        return false;
+    default: return false;
+    }
+}
+
+// coefficient k * X_q (or X_q * k) -> (k, q)
+bool split_linear_coef(const ExprP& c, ExprP& k, int& q) {
+    if (c->op == Op::Var && c->vk == VarKind::Process) {
+        k = mk_const(1.0);
+        q = c->idx;
+        return true;
+    }
+    if (c->op != Op::Mul) return false;
+    const ExprP& a = c->args[0];
+    const ExprP& b = c->args[1];
+    if (b->op == Op::Var && b->vk == VarKind::Process) { k = a; q = b->idx; return true; }
+    if (a->op == Op::Var && a->vk == VarKind::Process) { k = b; q = a->idx; return true; }
+    return false;
+}
+
+// Constant diffusion matrix K[p][j] (process p, Wiener index j) of a
+// universe whose every dW term is constant * own process; false otherwise.
+bool diffusion_matrix(const Universe& u, std::vector<std::vector<double>>& K) {
+    const int P = u.n_processes(), NI = u.n_stochastic();
+    K.assign(P, std::vector<double>(NI, 0.0));
+    bool any = false;
+    for (int p = 0; p < P; ++p)
+        for (const auto& t : u.procs[p].terms) {
+            if (t.kind != IncKind::Dw) continue;
+            ExprP k;
+            int q = -1;
+            double v = 0.0;
+            if (!split_linear_coef(t.coef, k, q) || q != p || !fold_const(k, v)) return false;
+            K[p][t.sidx] += v;
+            any = true;
+        }
+    return any;
+}
 
 enum class Mode { Forward, Batch };
 
@@ -341,25 +399,15 @@ struct Gen {
 
     // coefficient k * X_q (or X_q * k) -> (k, q); k may be any expression:
     // sum_j (k_j X_q) inc_j = X_q sum_j k_j inc_j holds whatever k_j is
-    static bool split_linear(const ExprP& c, ExprP& k, int& q) {
-        if (c->op == Op::Var && c->vk == VarKind::Process) {
-            k = mk_const(1.0);
-            q = c->idx;
-            return true;
-        }
-        if (c->op != Op::Mul) return false;
-        const ExprP& a = c->args[0];
-        const ExprP& b = c->args[1];
-        if (b->op == Op::Var && b->vk == VarKind::Process) { k = a; q = b->idx; return true; }
-        if (a->op == Op::Var && a->vk == VarKind::Process) { k = b; q = a->idx; return true; }
-        return false;
-    }
+    static bool split_linear(const ExprP& c, ExprP& k, int& q) { return split_linear_coef(c, k, q); }
 
     // Euler update of process p.  FP64 keeps the reference's term order
     // (val += c * inc per term).  FP32 factors coefficients k_j * X_q out of
     // the sum: X_q * (sum_j k_j inc_j), one FMA per term instead of two
-    // operations; the value changes only by rounding.
-    void euler_update(Out& o, int p, const std::string& procset) const {
+    // operations; the value changes only by rounding.  With mma_d set, the
+    // dW terms are already summed in mma_d (sum_j K_pj w_j from the tensor
+    // cores) and join the group of X_p.
+    void euler_update(Out& o, int p, const std::string& procset, const std::string& mma_d = "") const {
         o.l(R + " " + V("N", p) + " = " + V("X", p) + ";");
         const auto& terms = u.procs[p].terms;
         if (!f32) {
@@ -369,9 +417,14 @@ struct Gen {
         }
         std::vector<int> groups;
         std::vector<std::vector<std::pair<ExprP, std::string>>> gterms;
+        if (!mma_d.empty()) {
+            groups.push_back(p);
+            gterms.emplace_back();
+        }
         for (const auto& t : terms) {
             ExprP k;
             int q;
+            if (!mma_d.empty() && t.kind == IncKind::Dw) continue;
             if (split_linear(t.coef, k, q)) {
                 auto it = std::find(groups.begin(), groups.end(), q);
                 size_t gi = it - groups.begin();
@@ -383,7 +436,7 @@ struct Gen {
         }
         for (size_t g = 0; g < groups.size(); ++g) {
             const std::string acc = V("acc" + S(p) + "_", (int)g);
-            o.l(R + " " + acc + " = " + L(0.0) + ";");
+            o.l(R + " " + acc + " = " + (!mma_d.empty() && g == 0 ? mma_d : L(0.0)) + ";");
             for (const auto& kt : gterms[g]) o.l(acc + " = " + acc + " + " + ex(kt.first, procset, "tc") + " * " + kt.second + ";");
             o.l(V("N", p) + " = " + V("N", p) + " + " + V(procset, groups[g]) + " * " + acc + ";");
         }
@@ -481,8 +534,150 @@ struct Gen {
     }
 
     void step(Out& o) const {
-        if (sp.semantics == SEM_TEXTBOOK) step_textbook(o);
+        if (mma) step_mma(o);
+        else if (sp.semantics == SEM_TEXTBOOK) step_textbook(o);
         else step_reference(o);
+    }
+
+    // ---- one Euler step with the dW terms on the tensor cores -------------
+    // Eligible universes have no algebraic process, so the reference's cache
+    // equals the state at t under both semantics (euler.rs:5-37).  The CTA's
+    // 128 paths write their Wiener increments (split into TF32 hi + lo) as
+    // rows of A; one thread issues D = A_hi B_hi + A_hi B_lo + A_lo B_hi
+    // (3xTF32, about FP32 accuracy) into tensor memory; each thread reads
+    // back its row d_p = sum_j K_pj w_j and finishes the update in FP32.
+    const MmaShape* mma = nullptr;
+    void step_mma(Out& o) const {
+        const int KP = mma->kpad, NP = mma->npad;
+        for (int k4 = 0; k4 < KP; k4 += 4) {
+            std::string e[4];
+            bool any = false;
+            for (int i = 0; i < 4; ++i) {
+                const int k = k4 + i;
+                const bool dw = k < NI && u.token_kind[k] == IncKind::Dw;
+                e[i] = dw ? V("w", k) : "0.0f";
+                any = any || dw;
+            }
+            if (!any) continue;  // stays zero from the prologue
+            const std::string off = S(k4 / 4 * 32);
+            o.l("{ const float4 wv = make_float4(" + e[0] + ", " + e[1] + ", " + e[2] + ", " + e[3] + ");");
+            o.l("  const float4 wh = make_float4(sde_tf32_hi(wv.x), sde_tf32_hi(wv.y), sde_tf32_hi(wv.z), "
+                "sde_tf32_hi(wv.w));");
+            o.l("  *(float4*)(ARH + " + off + ") = wh;");
+            o.l("  *(float4*)(ARL + " + off + ") = make_float4(wv.x - wh.x, wv.y - wh.y, wv.z - wh.z, wv.w - wh.w); }");
+        }
+        o.l("sde_fence_async_smem();");
+        o.l("sde_tc_fence_before();");
+        o.l("if (!__syncthreads_and(tc_ok)) { tc_fail = 1; break; }");
+        o.l("sde_tc_fence_after();");
+        o.l("if (threadIdx.x == 0) {");
+        for (int c = 0; c < KP / 8; ++c) {
+            const std::string dc = S(c * 16) + "ull";  // 256 bytes further along K, in 16-byte units
+            o.l("  sde_mma_tf32(tmem, ADH + " + dc + ", BDH + " + dc + ", IDESC, " + (c ? "1u" : "0u") + ");");
+            o.l("  sde_mma_tf32(tmem, ADH + " + dc + ", BDL + " + dc + ", IDESC, 1u);");
+            o.l("  sde_mma_tf32(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
+        }
+        o.l("  sde_mma_commit(MBAR);");
+        o.l("}");
+        o.l("tc_ok = sde_mbar_wait_bounded(MBAR, tc_phase) ? 1 : 0;");
+        o.l("tc_phase ^= 1u;");
+        o.l("__syncwarp();");
+        o.l("sde_tc_fence_after();");
+        o.l("float DM[" + S(NP) + "];");
+        for (int c = 0; c < NP / 16; ++c) o.l("sde_tmem_ld16_wait(TROW + " + S(c * 16) + "u, DM + " + S(c * 16) + ");");
+        for (int p : u.levy) o.l(V("C", p) + " = " + V("X", p) + ";");
+        poisson(o, "C", "tc");
+        for (int p : u.levy) euler_update(o, p, "C", "DM[" + S(p) + "]");
+        for (int p = 0; p < P; ++p) o.l(V("X", p) + " = " + V("N", p) + ";");
+    }
+
+    // Forward kernel on the tensor cores (one path per thread, 128 paths per
+    // CTA = the MMA's M).  Shared memory: A_hi, A_lo [128 x KP], B_hi, B_lo
+    // [NP x KP], all in the no-swizzle K-major core-matrix layout; element
+    // (r, k) at (r/8)*(8 KP) + (k/4)*32 + (r%8)*4 + k%4 floats.  D [128 x NP]
+    // FP32 in tensor memory.  Every wait is bounded: on a timeout the CTA
+    // stops stepping, frees its tensor memory and sets *a.status.
+    std::string forward_mma(const std::string& name, const std::vector<std::vector<double>>& K) {
+        mode = Mode::Forward;
+        lane(0);
+        const int KP = mma->kpad, NP = mma->npad;
+        const int NPAY = (int)sp.payoffs.size();
+        Out o;
+        // B_hi then B_lo as one shared-memory image
+        std::vector<float> img(2 * (size_t)NP * KP, 0.0f);
+        for (int n = 0; n < P; ++n)
+            for (int k = 0; k < NI; ++k) {
+                const float kf = (float)K[n][k];
+                uint32_t bits;
+                std::memcpy(&bits, &kf, 4);
+                bits &= 0xFFFFE000u;
+                float hi;
+                std::memcpy(&hi, &bits, 4);
+                const size_t at = (size_t)(n / 8) * (8 * KP) + (k / 4) * 32 + (n % 8) * 4 + k % 4;
+                img[at] = hi;
+                img[(size_t)NP * KP + at] = kf - hi;
+            }
+        o.l("static __device__ __align__(16) const float " + name + "_kmat[" + S((int)img.size()) + "] = {");
+        for (size_t i = 0; i < img.size(); i += 8) {
+            std::string row = "  ";
+            for (size_t j = i; j < std::min(img.size(), i + 8); ++j) row += lit(img[j], true) + ", ";
+            o.l(row);
+        }
+        o.l("};");
+        o.l("extern \"C\" __global__ void __launch_bounds__(128) " + name + "(const sde_args a) {");
+        o.ind++;
+        o.l("extern __shared__ __align__(1024) unsigned char sde_smem[];");
+        o.l("float* const SAH = (float*)sde_smem;");
+        o.l("float* const SAL = SAH + " + S(128 * KP) + ";");
+        o.l("float* const SBH = SAL + " + S(128 * KP) + ";");
+        o.l("sde_u64* const MBP = (sde_u64*)(SBH + " + S(2 * NP * KP) + ");");
+        o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 1);");
+        o.l("const sde_u32 MBAR = sde_smem_addr(MBP);");
+        o.l("for (int e = threadIdx.x; e < " + S(2 * 128 * KP / 4) + "; e += 128) ((float4*)SAH)[e] = make_float4(0.f, 0.f, 0.f, 0.f);");
+        o.l("for (int e = threadIdx.x; e < " + S(2 * NP * KP / 4) + "; e += 128) ((float4*)SBH)[e] = ((const float4*)" +
+            name + "_kmat)[e];");
+        o.l("if (threadIdx.x == 0) { sde_mbar_init(MBAR, 1u); sde_fence_mbar_init(); }");
+        o.l("__syncwarp();");
+        o.l("if (threadIdx.x < 32) sde_tmem_alloc(sde_smem_addr(TSLOT), " + S(mma->ncols) + "u);");
+        o.l("sde_fence_async_smem();");
+        o.l("sde_tc_fence_before();");
+        o.l("__syncthreads();");
+        o.l("sde_tc_fence_after();");
+        o.l("const sde_u32 tmem = *TSLOT;");
+        o.l("const sde_u32 TROW = tmem + ((sde_u32)(threadIdx.x & ~31u) << 16);");
+        o.l("const sde_u32 IDESC = sde_idesc_tf32(128, " + S(NP) + ");");
+        o.l("const sde_u64 ADH = sde_smem_desc(sde_smem_addr(SAH), 128u, " + S(KP * 32) + "u);");
+        o.l("const sde_u64 ADL = sde_smem_desc(sde_smem_addr(SAL), 128u, " + S(KP * 32) + "u);");
+        o.l("const sde_u64 BDH = sde_smem_desc(sde_smem_addr(SBH), 128u, " + S(KP * 32) + "u);");
+        o.l("const sde_u64 BDL = sde_smem_desc(sde_smem_addr(SBH + " + S(NP * KP) + "), 128u, " + S(KP * 32) + "u);");
+        o.l("float* const ARH = SAH + (threadIdx.x >> 3) * " + S(8 * KP) + " + (threadIdx.x & 7) * 4;");
+        o.l("float* const ARL = ARH + " + S(128 * KP) + ";");
+        o.l("int tc_ok = 1, tc_fail = 0;");
+        o.l("sde_u32 tc_phase = 0u;");
+        o.l("(void)tc_fail;");
+        shared_prologue(o);
+        lane_prologue(o);
+        store(o, "0");
+        time_loop(o);
+        // teardown: every thread arrives here (the break above is block-uniform)
+        o.l("sde_tc_fence_before();");
+        o.l("const int tc_all = __syncthreads_and(tc_ok);");
+        o.l("sde_tc_fence_after();");
+        o.l("if (threadIdx.x < 32) {");
+        o.l("  if (!tc_all) (void)sde_mbar_wait_bounded(MBAR, tc_phase ^ 1u);");
+        o.l("  __syncwarp();");
+        o.l("  sde_tmem_dealloc(tmem, " + S(mma->ncols) + "u);");
+        o.l("}");
+        o.l("if (!tc_all && threadIdx.x == 0 && a.status) atomicOr(a.status, 1);");
+        if (NPAY > 0) {
+            o.l("double fs[" + S(NPAY) + "] = {}, fq[" + S(NPAY) + "] = {};");
+            payoffs(o, NPAY);
+            o.l("sde_block_reduce_store<" + S(NPAY) + ">(fs, fq, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " +
+                S(NPAY) + "u) * 4u);");
+        }
+        o.ind--;
+        o.l("}");
+        return o.s.str();
     }
 
     void store(Out& o, const std::string& tidx) const {
@@ -808,12 +1003,41 @@ static std::string tag(const KernelSpec& s) {
     return r;
 }
 
-std::string forward_kernel_name(const KernelSpec& s) { return "sde_step_" + tag(s); }
+MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
+    MmaShape m;
+    if (s.precision != PREC_FP32 || s.scheme != SCHEME_EULER || s.adjoint || s.ppt != 1 || !u.alg.empty()) return m;
+    std::vector<std::vector<double>> K;
+    if (!diffusion_matrix(u, K)) return m;
+    m.npad = std::max(16, (u.n_processes() + 15) / 16 * 16);   // M = 128 takes N = 16..256 in steps of 16
+    m.kpad = std::max(8, (u.n_stochastic() + 7) / 8 * 8);      // K = 8 per TF32 MMA
+    if (m.npad > 256) return m;
+    m.ncols = 32;
+    while (m.ncols < m.npad) m.ncols *= 2;
+    const int need = 2 * 128 * m.kpad * 4 + 2 * m.npad * m.kpad * 4 + 16;
+    // at most 512 / ncols CTAs of an SM can hold tensor memory at once: ask
+    // for enough shared memory (228 KB per SM) that no more are resident
+    const int floor_bytes = 233472 / (512 / m.ncols + 1) + 1;
+    m.smem_bytes = std::max(need, floor_bytes);
+    if (m.smem_bytes > 227 * 1024) return m;
+    m.eligible = true;
+    return m;
+}
+
+std::string forward_kernel_name(const KernelSpec& s) { return "sde_step_" + tag(s) + (s.tensor_cores ? "_tc" : ""); }
 std::string adjoint_kernel_name(const KernelSpec& s) { return "sde_adjoint_" + tag(s); }
 
 std::string generate_source(const Universe& u, const KernelSpec& s) {
     Gen g(u, s);
     std::string src;
+    if (s.tensor_cores) {
+        const MmaShape m = mma_shape(u, s);
+        std::vector<std::vector<double>> K;
+        if (!m.eligible || !diffusion_matrix(u, K) || s.block != 128)
+            throw std::runtime_error("the universe is not eligible for the tensor-core lowering");
+        g.mma = &m;
+        src += g.forward_mma(forward_kernel_name(s), K);
+        return src;
+    }
     src += g.forward(forward_kernel_name(s));
     if (s.adjoint) {
         KernelSpec s1 = s;

@@ -25,12 +25,26 @@ struct KernelSpec {
     int block = 256;
     int ppt = 1;                        // paths per thread (independent chains)
     int icdf = 0;                       // 0: AS 26.2.23 (reference), 1: accurate
+    int tensor_cores = 0;               // 1: correlated diffusions on tcgen05 when eligible
     // adjoint: parameters and initial values to differentiate
     bool adjoint = false;
     std::vector<int> grad_params;       // parameter indices
     std::vector<int> grad_x0;           // process indices
     int ckpt_every = 19;                // steps between adjoint checkpoints
 };
+
+// Tensor-core lowering of correlated diffusions: eligible when the plan is
+// FP32 Euler, forward, one path per thread, without algebraic processes,
+// and every dW coefficient is a constant times its own process.  Then the
+// per-step increments are D = W K^T (paths x processes) on tcgen05.
+struct MmaShape {
+    bool eligible = false;
+    int npad = 0;         // processes padded to a multiple of 16 (MMA N)
+    int kpad = 0;         // Wiener indices padded to a multiple of 8 (MMA K)
+    int ncols = 0;        // tensor-memory columns allocated (power of 2 >= 32)
+    int smem_bytes = 0;   // dynamic shared memory of the kernel
+};
+MmaShape mma_shape(const Universe& u, const KernelSpec& s);
 
 // Name of the forward kernel in the generated source.
 std::string forward_kernel_name(const KernelSpec& s);

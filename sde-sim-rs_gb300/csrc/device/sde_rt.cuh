@@ -404,6 +404,22 @@ SDE_DEV void sde_tmem_ld16(sde_u32 taddr, float* d) {
     for (int i = 0; i < 16; ++i) d[i] = __uint_as_float(r[i]);
 }
 SDE_DEV void sde_tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+/* the same load with its wait in one statement, so no use of the registers
+ * can be scheduled between the two */
+SDE_DEV void sde_tmem_ld16_wait(sde_u32 taddr, float* d) {
+    sde_u32 r[16];
+    asm volatile(
+        "{\n\ttcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];\n\ttcgen05.wait::ld.sync.aligned;\n\t}"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) d[i] = __uint_as_float(r[i]);
+}
+/* makes an mbarrier.init visible to the async proxy (tensor-core commits) */
+SDE_DEV void sde_fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 /* TF32 split x = hi + lo (hi keeps the 19 bits a TF32 operand reads) */
 SDE_DEV float sde_tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }

@@ -313,6 +313,7 @@ struct sde_plan {
     sde::KernelSpec spec;
     int output = SDE_OUT_FULL;
     bool auto_block = true;  // block size chosen per run from the path count
+    int mma_smem = 0;        // dynamic shared memory of a tensor-core forward kernel
     std::string source;
     std::string fwd_name, adj_name;
     std::shared_ptr<sde::Cubin> cubin;
@@ -336,7 +337,7 @@ struct sde_result {
     sde::HBuf stage;               // pinned inputs, alive until the run is done
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
-    int* status_dev = nullptr;
+    sde::DBuf status;              // kernel status word (tensor-core waits)
     sde::HBuf status_host;
     bool waited = false;
 };
@@ -353,6 +354,10 @@ static Loaded& ensure_loaded(sde_plan* p) {
                                        nullptr, 0),
                    "cudaLibraryLoadData");
         cuda_check(cudaLibraryGetKernel(&L.fwd, L.lib, p->fwd_name.c_str()), "cudaLibraryGetKernel");
+        if (p->mma_smem > 0)
+            cuda_check(cudaKernelSetAttributeForDevice(L.fwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       p->mma_smem, dev),
+                       "tensor-core kernel shared memory");
         if (p->spec.adjoint)
             cuda_check(cudaLibraryGetKernel(&L.adj, L.lib, p->adj_name.c_str()), "cudaLibraryGetKernel");
     }
@@ -383,6 +388,8 @@ static KernelSpec spec_from(const sde_options* o) {
     s.ppt = o->paths_per_thread > 0 ? o->paths_per_thread : 1;
     s.icdf = o->icdf;
     if (s.icdf != SDE_ICDF_AS26 && s.icdf != SDE_ICDF_ACCURATE) fail(SDE_ERR_INVALID, "unknown icdf");
+    s.tensor_cores = o->tensor_cores;
+    if (s.tensor_cores != SDE_TC_OFF && s.tensor_cores != SDE_TC_ON) fail(SDE_ERR_INVALID, "unknown tensor_cores");
     if (s.ppt != 1 && s.ppt != 2 && s.ppt != 4) fail(SDE_ERR_INVALID, "paths_per_thread must be 1, 2 or 4");
     if (s.ckpt_every > 256) fail(SDE_ERR_INVALID, "ckpt_every must be at most 256");
     return s;
@@ -417,6 +424,18 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
         }
     }
     if (n_estimates(p.get()) > 32) fail(SDE_ERR_INVALID, "at most 32 payoffs and gradients");
+    if (p->spec.tensor_cores) {
+        // tcgen05 lowering where the universe allows it; the CUDA-core
+        // kernel otherwise
+        const MmaShape m = mma_shape(p->u, p->spec);
+        if (m.eligible) {
+            p->spec.block = 128;  // one MMA row per thread
+            p->auto_block = false;
+            p->mma_smem = m.smem_bytes;
+        } else {
+            p->spec.tensor_cores = 0;
+        }
+    }
     p->fwd_name = forward_kernel_name(p->spec);
     p->adj_name = adjoint_kernel_name(p->spec);
     p->source = generate_source(p->u, p->spec);
@@ -601,12 +620,24 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         A.ckpt = r->ckpt.as<float>();
     }
 
+    const bool tc = p->spec.tensor_cores && !p->spec.adjoint;
+    if (tc && N > 0) {
+        r->status = DBuf(16);
+        r->status_host = HBuf(16);
+        *r->status_host.as<int>() = 0;
+        cuda_check(cudaMemsetAsync(r->status.p, 0, 16, r->stream), "status word");
+        A.status = r->status.as<int>();
+    }
+
     if (N > 0 && T >= 1) {
         void* kargs[] = {&A};
         cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : L.fwd),
-                                    dim3((unsigned)gx, (unsigned)a.n_replicates), dim3(block), kargs, 0,
-                                    r->stream),
+                                    dim3((unsigned)gx, (unsigned)a.n_replicates), dim3(block), kargs,
+                                    tc ? (size_t)p->mma_smem : 0, r->stream),
                    "step kernel launch");
+        if (tc)
+            cuda_check(cudaMemcpyAsync(r->status_host.p, r->status.p, 4, cudaMemcpyDeviceToHost, r->stream),
+                       "status D2H");
         if (r->K > 0) {
             cuda_check(launch_reduce_partials(r->partials.as<double>(), (int)gx, r->K, a.n_replicates,
                                               r->est_dev.as<double>(), r->stream),
@@ -624,9 +655,12 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
 }
 
 static void wait(sde_result* r) {
-    if (r->waited) return;
-    cuda_check(cudaEventSynchronize(r->done), "kernel execution");
-    r->waited = true;
+    if (!r->waited) {
+        cuda_check(cudaEventSynchronize(r->done), "kernel execution");
+        r->waited = true;
+    }
+    if (r->status_host.p && *r->status_host.as<int>() != 0)
+        fail(SDE_ERR_DEVICE, "a tensor-core wait in the step kernel timed out; the run's values are not valid");
 }
 
 }  // namespace sde
@@ -791,6 +825,13 @@ int sde_plan_compile_log(const sde_plan* p, char* buf, size_t n, size_t* needed)
         const std::string& s = p->cubin->log;
         if (needed) *needed = s.size() + 1;
         if (buf && n) std::snprintf(buf, n, "%s", s.c_str());
+    });
+}
+
+int sde_plan_tensor_cores(const sde_plan* p, int32_t* on) {
+    return guarded([&] {
+        if (!p || !on) fail(SDE_ERR_INVALID, "NULL argument");
+        *on = p->spec.tensor_cores && !p->spec.adjoint ? 1 : 0;
     });
 }
 
@@ -1029,6 +1070,7 @@ int plan_view(sde_plan* p, PlanView* v) {
         v->rng = p->spec.rng;
         v->scheme = p->spec.scheme;
         v->adjoint = p->spec.adjoint ? 1 : 0;
+        v->tensor_cores = p->spec.tensor_cores ? 1 : 0;
     });
 }
 

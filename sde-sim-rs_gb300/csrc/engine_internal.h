@@ -19,6 +19,7 @@ struct PlanView {
     int rng;           // RNG_PSEUDO / RNG_SOBOL
     int scheme;        // SCHEME_EULER / SCHEME_RK
     int adjoint;       // 1 for adjoint plans
+    int tensor_cores;  // 1 if the forward kernel runs on tcgen05 (dynamic shared memory)
 };
 
 // Fills v for plan p, loading its module on the current device if needed.

@@ -99,6 +99,8 @@ extern "C" int sde_run_estimates_static(sde_plan* plan, const double* times, int
     const int rc = plan_view(plan, &v);  // first call on a device: loads the plan's kernels
     if (rc != SDE_OK) return rc;
     if (v.adjoint) return fail_with(SDE_ERR_UNSUPPORTED, "the static-scratch entry runs forward plans");
+    if (v.tensor_cores)
+        return fail_with(SDE_ERR_UNSUPPORTED, "the static-scratch entry runs CUDA-core plans (tensor_cores off)");
     if (v.rng != RNG_PSEUDO)
         return fail_with(SDE_ERR_UNSUPPORTED, "the static-scratch entry runs pseudo-random plans (Sobol tables are "
                                               "engine-allocated)");

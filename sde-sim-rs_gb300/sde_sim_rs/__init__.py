@@ -156,11 +156,14 @@ class Plan:
                  scramble: str = "shift", precision: str = "fp64", semantics: str = "reference",
                  output: str = "full", block_size: int = 0, grad_params: Sequence[str] | None = None,
                  grad_x0: Sequence[str] | None = None, ckpt_every: int = 0, paths_per_thread: int = 1,
-                 icdf: str = "as26"):
+                 icdf: str = "as26", tensor_cores: bool = False):
         """grad_params / grad_x0 make an adjoint plan: each run also returns
         the pathwise derivatives of E[payoffs[0]] with respect to those
         parameters and initial values (Euler-Maruyama, checkpoints every
-        ckpt_every steps, default 19)."""
+        ckpt_every steps, default 19).  tensor_cores=True lowers the dW
+        terms of an FP32 Euler universe whose diffusions are constant * own
+        process (correlated GBM) to one tcgen05 product per 128 paths;
+        ``uses_tensor_cores`` says whether the universe was eligible."""
         if scheme not in N.SCHEME:
             raise ValueError(f"unknown scheme '{scheme}'")
         opts = N.Options()
@@ -175,6 +178,7 @@ class Plan:
         opts.ckpt_every = ckpt_every
         opts.paths_per_thread = paths_per_thread
         opts.icdf = N.ICDF[icdf]
+        opts.tensor_cores = 1 if tensor_cores else 0
         self.equations = list(equations)
         self.params = list(params)
         self.payoffs = list(payoffs)
@@ -202,6 +206,8 @@ class Plan:
         self.n_processes = n.value
         N.check(N.lib().sde_plan_n_stochastic(h, C.byref(n)))
         self.n_stochastic = n.value
+        N.check(N.lib().sde_plan_tensor_cores(h, C.byref(n)))
+        self.uses_tensor_cores = bool(n.value)
         buf = C.create_string_buffer(4096)
         self.process_names = []
         for i in range(self.n_processes):

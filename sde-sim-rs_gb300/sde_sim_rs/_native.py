@@ -35,7 +35,8 @@ class Options(C.Structure):
     _fields_ = [("struct_size", C.c_uint32), ("scheme", C.c_int32), ("rng", C.c_int32),
                 ("scramble", C.c_int32), ("precision", C.c_int32), ("semantics", C.c_int32),
                 ("output", C.c_int32), ("block_size", C.c_int32), ("ckpt_every", C.c_int32),
-                ("paths_per_thread", C.c_int32), ("icdf", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("paths_per_thread", C.c_int32), ("icdf", C.c_int32), ("tensor_cores", C.c_int32),
+                ("reserved", C.c_int32 * 4)]
 
 
 class RunArgs(C.Structure):
@@ -85,6 +86,7 @@ SIGNATURES = {
     "sde_plan_stochastic_token": ([C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t], C.c_int),
     "sde_plan_source": ([C.c_void_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
     "sde_plan_compile_log": ([C.c_void_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
+    "sde_plan_tensor_cores": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
     "sde_run": ([C.c_void_p, C.POINTER(RunArgs), C.POINTER(C.c_void_p)], C.c_int),
     "sde_simulate": ([C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_double), C.c_int32,
                       C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.c_int32, C.c_uint64,

@@ -174,6 +174,38 @@ def test_batch_lowering_compiles(engine):
         Batch([tg, engine.Plan(["dX = (0.1) * dW1"], payoffs=["X"], precision="fp64")])
 
 
+@pytest.mark.parametrize("rng,scramble", [("pseudo", "shift"), ("sobol", "xor"), ("sobol", "shift")])
+def test_tensor_core_lowering(engine, rng, scramble):
+    """Correlated GBM baskets lower to tcgen05 (3 TF32 MMAs per 8 Wiener
+    indices, 128 paths per CTA); other universes keep the CUDA-core kernel."""
+    from bench import basket_equations
+    eqs, payoff, _, _ = basket_equations(12)
+    p = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=rng, scramble=scramble, tensor_cores=True)
+    assert p.uses_tensor_cores
+    src = p.source
+    assert "_tc(const sde_args a)" in src and "__launch_bounds__(128)" in src
+    # K padded to 16 = 2 chunks of 8, 3 MMAs each, per unrolled step
+    n_mma = src.count("sde_mma_tf32(")
+    assert n_mma > 0 and n_mma % 6 == 0 and n_mma == 6 * src.count("sde_mma_commit(")
+    assert "sde_idesc_tf32(128, 16)" in src               # N = 12 processes padded to 16
+    assert "sde_mbar_wait_bounded" in src and "sde_tmem_dealloc" in src
+    # a coefficient of 1 * X and a folded constant are eligible too
+    q = engine.Plan(["dA = (0.01 * A) * dt + A * dW1 + ((0.5 * 0.2) * A) * dW2",
+                     "dB = (0.3 * B) * dW2"], payoffs=["A + B"], precision="fp32", tensor_cores=True)
+    assert q.uses_tensor_cores
+    # not eligible: state-dependent diffusion, FP64, Runge-Kutta, a cross term,
+    # an algebraic process, several paths per thread
+    for eqs2, kw in [(HESTON, {}), (EXAMPLE_GBM, {"precision": "fp64"}), (EXAMPLE_GBM, {"scheme": "runge-kutta"}),
+                     (["dA = (0.2 * B) * dW1", "dB = (0.1 * B) * dW1"], {}),
+                     (["dA = (0.2 * A) * dW1", "B = max(A - 1, 0)"], {}),
+                     (EXAMPLE_GBM, {"paths_per_thread": 2}),
+                     (["dA = (s * A) * dW1"], {"params": ["s"]})]:
+        kw.setdefault("precision", "fp32")
+        r = engine.Plan(eqs2, tensor_cores=True, **kw)
+        assert not r.uses_tensor_cores, (eqs2, kw)
+        assert "_tc(" not in r.source
+
+
 @pytest.mark.parametrize("ppt", [2, 4])
 def test_paths_per_thread_lowering(engine, ppt):
     from sde_sim_rs import _native as N

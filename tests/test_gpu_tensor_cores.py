@@ -1,0 +1,94 @@
+"""tcgen05 lowering of correlated GBM baskets (every dW coefficient is a
+constant times its own process).  The tensor-core kernel draws the same
+increments as the CUDA-core FP32 kernel and differs from it only by the
+3xTF32 product's rounding; against the FP64 oracle it meets the bar of the
+other FP32 kernels."""
+import math
+
+import numpy as np
+import pytest
+
+from bench import basket_equations
+
+pytestmark = pytest.mark.gpu
+
+THREADS = 8
+RNGS = {"pseudo": ("pseudo", "shift"), "sobol_xor": ("sobol", "xor"), "sobol_shift": ("sobol", "shift")}
+
+
+def _init(dim):
+    return {f"S{i + 1}": 100.0 for i in range(dim)}
+
+
+@pytest.mark.parametrize("dim", [4, 20, 64])
+@pytest.mark.parametrize("rng", list(RNGS))
+def test_tensor_core_paths_match_cuda_core_kernel(engine, dim, rng):
+    eqs, payoff, _, _ = basket_equations(dim)
+    r, s = RNGS[rng]
+    times = np.linspace(0.0, 1.0, 33)
+    n, reps = 1000, 2  # 1000 = 7 full CTAs of 128 paths and a ragged one
+    tc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=r, scramble=s, tensor_cores=True)
+    cc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=r, scramble=s)
+    assert tc.uses_tensor_cores and not cc.uses_tensor_cores
+    a = tc.run(times, _init(dim), n, replicates=reps, seed=5)
+    b = cc.run(times, _init(dim), n, replicates=reps, seed=5)
+    va, vb = a.values(), b.values()
+    assert va.shape == vb.shape == (reps, n, len(times), dim)
+    assert np.all(np.isfinite(va))
+    rel = np.abs(va - vb) / np.abs(vb)
+    # 3xTF32 keeps about FP32 accuracy per step; 32 steps of GBM
+    assert rel.max() < 2e-5, np.percentile(rel, [50, 99, 100])
+    sa, qa = a.estimates()
+    sb, qb = b.estimates()
+    assert np.allclose(sa, sb, rtol=2e-5) and np.allclose(qa, qb, rtol=4e-5)
+
+
+@pytest.mark.parametrize("rng", ["pseudo", "sobol_xor"])
+def test_tensor_core_basket_against_fp64_oracle(engine, oracle, rng):
+    dim = 8
+    eqs, _, _, _ = basket_equations(dim)
+    r, s = RNGS[rng]
+    times = np.linspace(0.0, 1.0, 17)
+    n, seed = 640, 11
+    plan = engine.Plan(eqs, precision="fp32", rng=r, scramble=s, output="terminal", tensor_cores=True)
+    assert plan.uses_tensor_cores
+    gpu = plan.run(times, _init(dim), n, seed=seed).values("reference")[0, :, 0, :]
+    cfg = dict(rng=oracle.PSEUDO) if r == "pseudo" else dict(rng=oracle.SOBOL, scramble=oracle.XOR)
+    ref = oracle.Universe(eqs).simulate(times, _init(dim), 0, n, seed=seed, n_per_replicate=n, full=False,
+                                        threads=THREADS, **cfg)
+    rel = np.abs(gpu - ref) / np.abs(ref)
+    # the same random inputs: every path agrees to FP32 accuracy
+    assert np.mean(rel < 1e-3) > 0.99, np.percentile(rel, [50, 99, 100])
+    for p in range(dim):
+        se = ref[:, p].std() / math.sqrt(n)
+        assert abs(gpu[:, p].mean() - ref[:, p].mean()) <= 3 * se
+
+
+def test_tensor_core_checkpoint_output_and_no_steps(engine):
+    dim = 16
+    eqs, payoff, _, _ = basket_equations(dim)
+    tc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng="sobol", scramble="xor",
+                     output="checkpoints", tensor_cores=True)
+    cc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng="sobol", scramble="xor",
+                     output="checkpoints")
+    times = np.linspace(0.0, 2.0, 65)
+    ck = [0, 16, 32, 64]
+    a = tc.run(times, _init(dim), 4096, seed=3, checkpoints=ck).values()
+    b = cc.run(times, _init(dim), 4096, seed=3, checkpoints=ck).values()
+    assert np.max(np.abs(a - b) / np.abs(b)) < 4e-5
+    # a single time point: no step, no MMA issued, tensor memory still freed
+    one = tc.run([0.0], _init(dim), 300, seed=3, checkpoints=[0]).values()
+    assert np.all(one == 100.0)
+
+
+def test_static_scratch_entry_refuses_tensor_core_plans(engine):
+    from sde_sim_rs import _native as N
+    eqs, payoff, _, _ = basket_equations(4)
+    tc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", tensor_cores=True)
+    times = np.linspace(0.0, 1.0, 5)
+    x0 = np.full(4, 100.0)
+    hs = np.zeros(1)
+    hq = np.zeros(1)
+    rc = N.lib().sde_run_estimates_static(tc._h, times.ctypes.data, len(times), x0.ctypes.data, 4, None, 0,
+                                          256, 1, 1, None, hs.ctypes.data, hq.ctypes.data)
+    assert rc == N.SDE_ERR_UNSUPPORTED
