@@ -456,7 +456,8 @@ def run_basket(args):
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     # the CUDA-core kernel (one FMA chain per process) and the tcgen05 one
-    # (the 64 x 64 diffusion product as 3xTF32 MMAs per 128 paths)
+    # (the 64 x 64 diffusion product as three FP16 MMAs per 16 indices and
+    # 128 paths, FP32 accumulation)
     legs = {}
     for leg, tc in (("cuda_cores", False), ("tensor_cores", True)):
         if tc and args.cuda_cores_only:
@@ -500,7 +501,7 @@ def run_basket(args):
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
              "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, estimator only"},
             {"paths": n, "steps": 128, "checkpoints": 32, "price": price, "price_se": se,
-             "kernel": "tcgen05 (3xTF32)" if main_leg["tc"] else "CUDA cores",
+             "kernel": "tcgen05 (3 x FP16 split, FP32 accumulate)" if main_leg["tc"] else "CUDA cores",
              "legs": {k: {"ms": v["ms"], "path_steps_per_s": ps / (v["ms"] * 1e-3), "price": v["price"],
                           "tensor_cores": v["tc"]} for k, v in legs.items()}})
 

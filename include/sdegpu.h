@@ -86,8 +86,9 @@ typedef struct sde_options {
 /* TC_ON: when the plan is FP32 Euler-Maruyama, forward, one path per
  * thread, without algebraic processes, and every dW coefficient is a
  * constant times its own process (correlated GBM baskets), the step's
- * Wiener terms run as one tcgen05 TF32 product per 128 paths (3xTF32,
- * about FP32 accuracy) and the block size is 128.  Other plans keep the
+ * Wiener terms run as one tcgen05 product per 128 paths (three FP16
+ * products of hi / lo splits, FP32 accumulation, about FP32 accuracy) and
+ * the block size is 128.  Other plans keep the
  * CUDA-core kernel; sde_plan_tensor_cores tells which was built.
  * No counterpart in the reference (its coefficient loop is
  * src/sim/euler.rs:17-33).                                                */

@@ -132,6 +132,37 @@ struct Out {
 
 std::string S(int v) { return std::to_string(v); }
 
+// IEEE binary16 from binary32, round to nearest even (subnormals kept).
+uint16_t f32_to_f16(float f) {
+    uint32_t x;
+    std::memcpy(&x, &f, 4);
+    const uint16_t sign = (uint16_t)((x >> 16) & 0x8000u);
+    const uint32_t ax = x & 0x7FFFFFFFu;
+    if (ax >= 0x7F800000u) return sign | (ax > 0x7F800000u ? 0x7E00u : 0x7C00u);
+    if (ax >= 0x477FF000u) return sign | 0x7C00u;  // 65520 and up round to infinity
+    if (ax >= 0x38800000u) {                        // normal: rebias, round 23 -> 10 bits
+        const uint32_t m = ax - 0x38000000u;
+        return sign | (uint16_t)((m + 0xFFFu + ((m >> 13) & 1u)) >> 13);
+    }
+    if (ax < 0x33000000u) return sign;              // below 2^-25: zero
+    const int e = (int)(ax >> 23);
+    const uint32_t mant = (ax & 0x7FFFFFu) | 0x800000u;
+    const int shift = 126 - e;                      // value * 2^24 = mant >> shift
+    uint32_t q = mant >> shift;
+    const uint32_t rem = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
+    if (rem > half || (rem == half && (q & 1u))) ++q;
+    return sign | (uint16_t)q;
+}
+
+float f16_to_f32(uint16_t h) {
+    const int e = (h >> 10) & 0x1F, m = h & 0x3FF;
+    float v;
+    if (e == 0) v = std::ldexp((float)m, -24);
+    else if (e == 31) v = m ? NAN : INFINITY;
+    else v = std::ldexp((float)(m | 0x400), e - 25);
+    return (h & 0x8000u) ? -v : v;
+}
+
 // Value of an expression that reads no variable (plain f64 arithmetic, as
 // fasteval evaluates it); false if it reads one or uses an unfolded call.
 bool fold_const(const ExprP& e, double& v) {
@@ -284,14 +315,16 @@ struct Gen {
         }
     }
 
-    void uniforms(Out& o, int g, std::vector<bool>& block_done) const {
-        for (int k = 0; k < NI; ++k) {
+    // uniforms of Wiener / jump indices k0 <= k < k1 (all by default)
+    void uniforms(Out& o, int g, std::vector<bool>& block_done, int k0 = 0, int k1 = -1) const {
+        if (k1 < 0) k1 = NI;
+        for (int k = k0; k < k1; ++k) {
             if (xorm()) {
                 // dimension t*NI + k = group base (a multiple of 32) + e
                 const int e = g * NI + k, c = e / 32, l = e % 32;
                 if (!block_done[c]) {
-                    o.l(V("hv", c) + " = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, chunk0 + " + S(c) + ", " +
-                        V("H") + ", lane);");
+                    o.l(V("hv", c) + " = " + (mma ? "sde_sobol_hi_unrolled" : "sde_sobol_hi") +
+                        "(a.sobol_vt, mask_rep, a.sobol_dims, chunk0 + " + S(c) + ", " + V("H") + ", lane);");
                     block_done[c] = true;
                 }
                 o.l("const sde_u32 " + V("y", k) + " = __shfl_sync(0xffffffffu, " + V("hv", c) + ", " + S(l) +
@@ -329,41 +362,45 @@ struct Gen {
     }
 
     // Wiener increments w<k> = sqrt_dt * icdf(u<k>)   (increment.rs:89-97)
-    void wiener(Out& o, bool from_words = false) const {
+    // for k0 <= k < k1; mult replaces sqrt_dt (the tensor-core step writes
+    // scaled standard normals and applies sqrt_dt to the product)
+    void wiener(Out& o, bool from_words = false, const std::string& mult = "sdt", int k0 = 0, int k1 = -1) const {
+        if (k1 < 0) k1 = NI;
         const bool acc = sp.icdf != 0;
         // FP32 with the AS 26.2.23 normal: pairs of Wiener indices share
         // paired FP32 arithmetic (fma.f32x2)
         // (wide universes -- dozens of normals per step feeding long FMA
-        // chains -- are register-bound already; pairing is kept to <= 16)
+        // chains -- are register-bound already; pairing is kept to <= 16,
+        // except where the normals stream into shared memory)
         std::vector<int> paired;
-        if (f32 && !acc && (from_words || !xorm()) && NI <= 16) {
+        if (f32 && !acc && (from_words || !xorm()) && (NI <= 16 || mma)) {
             std::vector<int> ks;
-            for (int k = 0; k < NI; ++k)
+            for (int k = k0; k < k1; ++k)
                 if (u.token_kind[k] == IncKind::Dw) ks.push_back(k);
             for (size_t i = 0; i + 1 < ks.size(); i += 2) {
                 const int ka = ks[i], kb = ks[i + 1];
                 const std::string pr = V("wp" + S(ka) + "_", kb);
                 const std::string src = xorm() ? "sde_normal_xor2(" + V("y", ka) + ", " + V("y", kb) + ")"
                                                 : "sde_normal_u53_2(" + V("U", ka) + ", " + V("U", kb) + ")";
-                o.l("const float2 " + pr + " = __fmul2_rn(make_float2(sdt, sdt), " + src + ");");
+                o.l("const float2 " + pr + " = __fmul2_rn(make_float2(" + mult + ", " + mult + "), " + src + ");");
                 o.l("const float " + V("w", ka) + " = " + pr + ".x;");
                 o.l("const float " + V("w", kb) + " = " + pr + ".y;");
                 paired.push_back(ka);
                 paired.push_back(kb);
             }
         }
-        for (int k = 0; k < NI; ++k) {
+        for (int k = k0; k < k1; ++k) {
             if (u.token_kind[k] != IncKind::Dw) continue;
             if (std::find(paired.begin(), paired.end(), k) != paired.end()) continue;
             if (!f32)
-                o.l("const double " + V("w", k) + " = sdt * " + (acc ? "sde_icdf_accurate(" : "sde_icdf_as26(") +
+                o.l("const double " + V("w", k) + " = " + mult + " * " + (acc ? "sde_icdf_accurate(" : "sde_icdf_as26(") +
                     V("u", k) + ");");
             else if (from_words && !acc)
-                o.l("const float " + V("w", k) + " = sdt * sde_normal_xor(" + V("y", k) + ");");
+                o.l("const float " + V("w", k) + " = " + mult + " * sde_normal_xor(" + V("y", k) + ");");
             else if (!xorm() && !acc)
-                o.l("const float " + V("w", k) + " = sdt * sde_normal_u53(" + V("U", k) + ");");
+                o.l("const float " + V("w", k) + " = " + mult + " * sde_normal_u53(" + V("U", k) + ");");
             else
-                o.l("const float " + V("w", k) + " = sdt * " + (acc ? "sde_icdf_accurate_q(" : "sde_icdf_as26_q(") +
+                o.l("const float " + V("w", k) + " = " + mult + " * " + (acc ? "sde_icdf_accurate_q(" : "sde_icdf_as26_q(") +
                     V("q", k) + ", " + V("up", k) + ");");
         }
     }
@@ -534,48 +571,54 @@ struct Gen {
     }
 
     void step(Out& o) const {
-        if (mma) step_mma(o);
-        else if (sp.semantics == SEM_TEXTBOOK) step_textbook(o);
+        if (sp.semantics == SEM_TEXTBOOK) step_textbook(o);
         else step_reference(o);
     }
 
     // ---- one Euler step with the dW terms on the tensor cores -------------
     // Eligible universes have no algebraic process, so the reference's cache
     // equals the state at t under both semantics (euler.rs:5-37).  The CTA's
-    // 128 paths write their Wiener increments (split into TF32 hi + lo) as
-    // rows of A; one thread issues D = A_hi B_hi + A_hi B_lo + A_lo B_hi
-    // (3xTF32, about FP32 accuracy) into tensor memory; each thread reads
-    // back its row d_p = sum_j K_pj w_j and finishes the update in FP32.
+    // 128 paths write their standard normals z (times 2^12, split into FP16
+    // hi + lo) as rows of A, eight indices at a time as they are drawn; one
+    // thread issues D = A_hi B_hi + A_hi B_lo + A_lo B_hi (3 FP16 products,
+    // about FP32 accuracy; B = K with each row scaled by a power of two)
+    // into tensor memory; each thread reads back its row and finishes the
+    // update in FP32 with d_p = D_p sqrt_dt 2^-(12 + e_p) = sum_j K_pj w_j.
     const MmaShape* mma = nullptr;
-    void step_mma(Out& o) const {
+    std::vector<int> row_e;   // B row p is K_p * 2^row_e[p]
+    void step_mma(Out& o, int g, std::vector<bool>& done) const {
         const int KP = mma->kpad, NP = mma->npad;
-        for (int k4 = 0; k4 < KP; k4 += 4) {
-            std::string e[4];
+        for (int k8 = 0; k8 < KP; k8 += 8) {
+            if (k8 < NI) {
+                uniforms(o, g, done, k8, std::min(k8 + 8, NI));
+                wiener(o, xorm() && f32, "0x1p12f", k8, std::min(k8 + 8, NI));
+            }
+            std::string e[8];
             bool any = false;
-            for (int i = 0; i < 4; ++i) {
-                const int k = k4 + i;
+            for (int i = 0; i < 8; ++i) {
+                const int k = k8 + i;
                 const bool dw = k < NI && u.token_kind[k] == IncKind::Dw;
                 e[i] = dw ? V("w", k) : "0.0f";
                 any = any || dw;
             }
             if (!any) continue;  // stays zero from the prologue
-            const std::string off = S(k4 / 4 * 32);
-            o.l("{ const float4 wv = make_float4(" + e[0] + ", " + e[1] + ", " + e[2] + ", " + e[3] + ");");
-            o.l("  const float4 wh = make_float4(sde_tf32_hi(wv.x), sde_tf32_hi(wv.y), sde_tf32_hi(wv.z), "
-                "sde_tf32_hi(wv.w));");
-            o.l("  *(float4*)(ARH + " + off + ") = wh;");
-            o.l("  *(float4*)(ARL + " + off + ") = make_float4(wv.x - wh.x, wv.y - wh.y, wv.z - wh.z, wv.w - wh.w); }");
+            const std::string off = S(k8 / 8 * 128);
+            o.l("{ sde_u32 h0, h1, h2, h3, l0, l1, l2, l3;");
+            for (int i = 0; i < 4; ++i)
+                o.l("  sde_split_f16x2(" + e[2 * i] + ", " + e[2 * i + 1] + ", h" + S(i) + ", l" + S(i) + ");");
+            o.l("  *(uint4*)(ARH + " + off + ") = make_uint4(h0, h1, h2, h3);");
+            o.l("  *(uint4*)(ARL + " + off + ") = make_uint4(l0, l1, l2, l3); }");
         }
         o.l("sde_fence_async_smem();");
         o.l("sde_tc_fence_before();");
         o.l("if (!__syncthreads_and(tc_ok)) { tc_fail = 1; break; }");
         o.l("sde_tc_fence_after();");
         o.l("if (threadIdx.x == 0) {");
-        for (int c = 0; c < KP / 8; ++c) {
+        for (int c = 0; c < KP / 16; ++c) {
             const std::string dc = S(c * 16) + "ull";  // 256 bytes further along K, in 16-byte units
-            o.l("  sde_mma_tf32(tmem, ADH + " + dc + ", BDH + " + dc + ", IDESC, " + (c ? "1u" : "0u") + ");");
-            o.l("  sde_mma_tf32(tmem, ADH + " + dc + ", BDL + " + dc + ", IDESC, 1u);");
-            o.l("  sde_mma_tf32(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
+            o.l("  sde_mma_f16(tmem, ADH + " + dc + ", BDH + " + dc + ", IDESC, " + (c ? "1u" : "0u") + ");");
+            o.l("  sde_mma_f16(tmem, ADH + " + dc + ", BDL + " + dc + ", IDESC, 1u);");
+            o.l("  sde_mma_f16(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
         }
         o.l("  sde_mma_commit(MBAR);");
         o.l("}");
@@ -585,56 +628,76 @@ struct Gen {
         o.l("sde_tc_fence_after();");
         o.l("float DM[" + S(NP) + "];");
         for (int c = 0; c < NP / 16; ++c) o.l("sde_tmem_ld16_wait(TROW + " + S(c * 16) + "u, DM + " + S(c * 16) + ");");
+        o.l("const float sdz = sdt * 0x1p-12f;");
         for (int p : u.levy) o.l(V("C", p) + " = " + V("X", p) + ";");
         poisson(o, "C", "tc");
-        for (int p : u.levy) euler_update(o, p, "C", "DM[" + S(p) + "]");
+        for (int p : u.levy) {
+            const std::string f = row_e[p] == 0 ? "sdz" : "(sdz * " + lit(std::ldexp(1.0, -row_e[p]), true) + ")";
+            euler_update(o, p, "C", "DM[" + S(p) + "] * " + f);
+        }
         for (int p = 0; p < P; ++p) o.l(V("X", p) + " = " + V("N", p) + ";");
     }
 
     // Forward kernel on the tensor cores (one path per thread, 128 paths per
     // CTA = the MMA's M).  Shared memory: A_hi, A_lo [128 x KP], B_hi, B_lo
-    // [NP x KP], all in the no-swizzle K-major core-matrix layout; element
-    // (r, k) at (r/8)*(8 KP) + (k/4)*32 + (r%8)*4 + k%4 floats.  D [128 x NP]
-    // FP32 in tensor memory.  Every wait is bounded: on a timeout the CTA
-    // stops stepping, frees its tensor memory and sets *a.status.
+    // [NP x KP] FP16, all in the no-swizzle K-major core-matrix layout
+    // (8 rows x 16 bytes per core matrix); element (r, k) at half
+    // (r/8)*(8 KP) + (k/8)*64 + (r%8)*8 + k%8.  D [128 x NP] FP32 in tensor
+    // memory.  Every wait is bounded: on a timeout the CTA stops stepping,
+    // frees its tensor memory and sets *a.status.
     std::string forward_mma(const std::string& name, const std::vector<std::vector<double>>& K) {
         mode = Mode::Forward;
         lane(0);
         const int KP = mma->kpad, NP = mma->npad;
         const int NPAY = (int)sp.payoffs.size();
         Out o;
+        // per-row power-of-two scale: the largest |K_pj 2^e_p| lies in
+        // [2^12, 2^13), so FP16 holds B_hi and the B_lo remainders
+        row_e.assign(P, 0);
+        for (int n = 0; n < P; ++n) {
+            double mx = 0.0;
+            for (int k = 0; k < NI; ++k) mx = std::max(mx, std::fabs(K[n][k]));
+            if (mx > 0.0) {
+                int ex = 0;
+                std::frexp(mx, &ex);  // mx < 2^ex
+                row_e[n] = std::max(-100, std::min(100, 13 - ex));
+            }
+        }
         // B_hi then B_lo as one shared-memory image
-        std::vector<float> img(2 * (size_t)NP * KP, 0.0f);
+        std::vector<uint16_t> img(2 * (size_t)NP * KP, 0);
         for (int n = 0; n < P; ++n)
             for (int k = 0; k < NI; ++k) {
-                const float kf = (float)K[n][k];
-                uint32_t bits;
-                std::memcpy(&bits, &kf, 4);
-                bits &= 0xFFFFE000u;
-                float hi;
-                std::memcpy(&hi, &bits, 4);
-                const size_t at = (size_t)(n / 8) * (8 * KP) + (k / 4) * 32 + (n % 8) * 4 + k % 4;
+                const float kf = (float)std::ldexp(K[n][k], row_e[n]);
+                const uint16_t hi = f32_to_f16(kf);
+                const uint16_t lo = f32_to_f16(kf - f16_to_f32(hi));
+                const size_t at = (size_t)(n / 8) * (8 * KP) + (k / 8) * 64 + (n % 8) * 8 + k % 8;
                 img[at] = hi;
-                img[(size_t)NP * KP + at] = kf - hi;
+                img[(size_t)NP * KP + at] = lo;
             }
-        o.l("static __device__ __align__(16) const float " + name + "_kmat[" + S((int)img.size()) + "] = {");
-        for (size_t i = 0; i < img.size(); i += 8) {
+        o.l("static __device__ __align__(16) const unsigned short " + name + "_kmat[" + S((int)img.size()) + "] = {");
+        for (size_t i = 0; i < img.size(); i += 16) {
             std::string row = "  ";
-            for (size_t j = i; j < std::min(img.size(), i + 8); ++j) row += lit(img[j], true) + ", ";
+            for (size_t j = i; j < std::min(img.size(), i + 16); ++j) {
+                char b[16];
+                std::snprintf(b, sizeof b, "0x%04x, ", img[j]);
+                row += b;
+            }
             o.l(row);
         }
         o.l("};");
-        o.l("extern \"C\" __global__ void __launch_bounds__(128) " + name + "(const sde_args a) {");
+        o.l("extern \"C\" __global__ void __launch_bounds__(128, " + S(mma->min_blocks) + ") " + name +
+            "(const sde_args a) {");
         o.ind++;
         o.l("extern __shared__ __align__(1024) unsigned char sde_smem[];");
-        o.l("float* const SAH = (float*)sde_smem;");
-        o.l("float* const SAL = SAH + " + S(128 * KP) + ";");
-        o.l("float* const SBH = SAL + " + S(128 * KP) + ";");
-        o.l("sde_u64* const MBP = (sde_u64*)(SBH + " + S(2 * NP * KP) + ");");
+        o.l("unsigned char* const SAH = sde_smem;");
+        o.l("unsigned char* const SAL = SAH + " + S(128 * KP * 2) + ";");
+        o.l("unsigned char* const SBH = SAL + " + S(128 * KP * 2) + ";");
+        o.l("unsigned char* const SBL = SBH + " + S(NP * KP * 2) + ";");
+        o.l("sde_u64* const MBP = (sde_u64*)(SBL + " + S(NP * KP * 2) + ");");
         o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 1);");
         o.l("const sde_u32 MBAR = sde_smem_addr(MBP);");
-        o.l("for (int e = threadIdx.x; e < " + S(2 * 128 * KP / 4) + "; e += 128) ((float4*)SAH)[e] = make_float4(0.f, 0.f, 0.f, 0.f);");
-        o.l("for (int e = threadIdx.x; e < " + S(2 * NP * KP / 4) + "; e += 128) ((float4*)SBH)[e] = ((const float4*)" +
+        o.l("for (int e = threadIdx.x; e < " + S(2 * 128 * KP * 2 / 16) + "; e += 128) ((uint4*)SAH)[e] = make_uint4(0u, 0u, 0u, 0u);");
+        o.l("for (int e = threadIdx.x; e < " + S(2 * NP * KP * 2 / 16) + "; e += 128) ((uint4*)SBH)[e] = ((const uint4*)" +
             name + "_kmat)[e];");
         o.l("if (threadIdx.x == 0) { sde_mbar_init(MBAR, 1u); sde_fence_mbar_init(); }");
         o.l("__syncwarp();");
@@ -645,13 +708,14 @@ struct Gen {
         o.l("sde_tc_fence_after();");
         o.l("const sde_u32 tmem = *TSLOT;");
         o.l("const sde_u32 TROW = tmem + ((sde_u32)(threadIdx.x & ~31u) << 16);");
-        o.l("const sde_u32 IDESC = sde_idesc_tf32(128, " + S(NP) + ");");
-        o.l("const sde_u64 ADH = sde_smem_desc(sde_smem_addr(SAH), 128u, " + S(KP * 32) + "u);");
-        o.l("const sde_u64 ADL = sde_smem_desc(sde_smem_addr(SAL), 128u, " + S(KP * 32) + "u);");
-        o.l("const sde_u64 BDH = sde_smem_desc(sde_smem_addr(SBH), 128u, " + S(KP * 32) + "u);");
-        o.l("const sde_u64 BDL = sde_smem_desc(sde_smem_addr(SBH + " + S(NP * KP) + "), 128u, " + S(KP * 32) + "u);");
-        o.l("float* const ARH = SAH + (threadIdx.x >> 3) * " + S(8 * KP) + " + (threadIdx.x & 7) * 4;");
-        o.l("float* const ARL = ARH + " + S(128 * KP) + ";");
+        // LBO: the two core matrices of one MMA's K slice; SBO: 8-row groups
+        o.l("const sde_u32 IDESC = sde_idesc_f16(128, " + S(NP) + ");");
+        o.l("const sde_u64 ADH = sde_smem_desc(sde_smem_addr(SAH), 128u, " + S(KP * 16) + "u);");
+        o.l("const sde_u64 ADL = sde_smem_desc(sde_smem_addr(SAL), 128u, " + S(KP * 16) + "u);");
+        o.l("const sde_u64 BDH = sde_smem_desc(sde_smem_addr(SBH), 128u, " + S(KP * 16) + "u);");
+        o.l("const sde_u64 BDL = sde_smem_desc(sde_smem_addr(SBL), 128u, " + S(KP * 16) + "u);");
+        o.l("unsigned char* const ARH = SAH + (threadIdx.x >> 3) * " + S(16 * KP) + " + (threadIdx.x & 7) * 16;");
+        o.l("unsigned char* const ARL = ARH + " + S(128 * KP * 2) + ";");
         o.l("int tc_ok = 1, tc_fail = 0;");
         o.l("sde_u32 tc_phase = 0u;");
         o.l("(void)tc_fail;");
@@ -783,9 +847,13 @@ struct Gen {
                 lane(j);
                 o.l("{");
                 o.ind++;
-                uniforms(o, g, done[j]);
-                wiener(o, xorm() && f32);
-                step(o);
+                if (mma) {
+                    step_mma(o, g, done[j]);
+                } else {
+                    uniforms(o, g, done[j]);
+                    wiener(o, xorm() && f32);
+                    step(o);
+                }
                 store(o, "t + 1");
                 o.ind--;
                 o.l("}");
@@ -1009,16 +1077,20 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
     std::vector<std::vector<double>> K;
     if (!diffusion_matrix(u, K)) return m;
     m.npad = std::max(16, (u.n_processes() + 15) / 16 * 16);   // M = 128 takes N = 16..256 in steps of 16
-    m.kpad = std::max(8, (u.n_stochastic() + 7) / 8 * 8);      // K = 8 per TF32 MMA
+    m.kpad = std::max(16, (u.n_stochastic() + 15) / 16 * 16);  // K = 16 per FP16 MMA
     if (m.npad > 256) return m;
     m.ncols = 32;
     while (m.ncols < m.npad) m.ncols *= 2;
-    const int need = 2 * 128 * m.kpad * 4 + 2 * m.npad * m.kpad * 4 + 16;
+    const int need = 2 * 128 * m.kpad * 2 + 2 * m.npad * m.kpad * 2 + 16;
     // at most 512 / ncols CTAs of an SM can hold tensor memory at once: ask
     // for enough shared memory (228 KB per SM) that no more are resident
     const int floor_bytes = 233472 / (512 / m.ncols + 1) + 1;
     m.smem_bytes = std::max(need, floor_bytes);
     if (m.smem_bytes > 227 * 1024) return m;
+    // CTAs per SM that the shared memory allows (1 KB reserved and 1 KB of
+    // static reduction scratch each), capped at 4: the register budget of
+    // __launch_bounds__
+    m.min_blocks = std::max(1, std::min(4, 233472 / (m.smem_bytes + 2048)));
     m.eligible = true;
     return m;
 }

@@ -40,9 +40,10 @@ struct KernelSpec {
 struct MmaShape {
     bool eligible = false;
     int npad = 0;         // processes padded to a multiple of 16 (MMA N)
-    int kpad = 0;         // Wiener indices padded to a multiple of 8 (MMA K)
+    int kpad = 0;         // Wiener indices padded to a multiple of 16 (MMA K)
     int ncols = 0;        // tensor-memory columns allocated (power of 2 >= 32)
     int smem_bytes = 0;   // dynamic shared memory of the kernel
+    int min_blocks = 1;   // CTAs per SM the kernel is register-budgeted for
 };
 MmaShape mma_shape(const Universe& u, const KernelSpec& s);
 

@@ -424,6 +424,47 @@ SDE_DEV void sde_fence_mbar_init() { asm volatile("fence.mbarrier_init.release.c
 /* TF32 split x = hi + lo (hi keeps the 19 bits a TF32 operand reads) */
 SDE_DEV float sde_tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
+/* instruction descriptor, kind::f16 with F16 A and B (both K-major) and an
+ * F32 accumulator */
+SDE_DEV sde_u32 sde_idesc_f16(int M, int N) {
+    return (1u << 4) | ((sde_u32)(N >> 3) << 17) | ((sde_u32)(M >> 4) << 24);
+}
+SDE_DEV void sde_mma_f16(sde_u32 dtmem, sde_u64 adesc, sde_u64 bdesc, sde_u32 idesc, sde_u32 accumulate) {
+    asm volatile(
+        "{ .reg .pred p; setp.ne.b32 p, %4, 0; tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p; }" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+/* FP16 split of two values: x = hi + lo with hi = f16(x) and lo = f16(x - hi)
+ * (x - hi is exact in FP32), packed with the first value in the low half. */
+SDE_DEV void sde_split_f16x2(float x0, float x1, sde_u32& hi, sde_u32& lo) {
+    asm("{\n\t.reg .b16 h0, h1;\n\t.reg .f32 f0, f1;\n\t"
+        "cvt.rn.f16x2.f32 %0, %3, %2;\n\t"
+        "mov.b32 {h0, h1}, %0;\n\t"
+        "cvt.f32.f16 f0, h0;\n\t"
+        "cvt.f32.f16 f1, h1;\n\t"
+        "sub.rn.f32 f0, %2, f0;\n\t"
+        "sub.rn.f32 f1, %3, f1;\n\t"
+        "cvt.rn.f16x2.f32 %1, f1, f0;\n\t}"
+        : "=&r"(hi), "=&r"(lo)
+        : "f"(x0), "f"(x1));
+}
+
+/* sde_sobol_hi with the direction-number loads unrolled over the bits H can
+ * hold (predicated), so they are in flight together instead of one per
+ * loop trip */
+SDE_DEV sde_u32 sde_sobol_hi_unrolled(const sde_u32* __restrict__ VT, const sde_u32* __restrict__ mask, int dims,
+                                      int chunk, sde_u32 H, int lane) {
+    const int d = chunk * 32 + lane;
+    if (d >= dims) return 0u;
+    sde_u32 acc = mask ? __ldg(mask + d) : 0u;
+    const sde_u32* col = VT + 5ull * (sde_u64)dims + (sde_u64)d;
+#pragma unroll
+    for (int b = 0; b < 27; ++b)
+        if ((H >> b) & 1u) acc ^= __ldg(col + (sde_u64)b * (sde_u64)dims);
+    return acc;
+}
+
 /* ------------------------------------------------------------------------
  * Estimator reduction (fused epilogue): warp shuffles, then a Neumaier
  * compensated sum over the block's warps, in FP64.  out gets

@@ -176,19 +176,37 @@ def test_batch_lowering_compiles(engine):
 
 @pytest.mark.parametrize("rng,scramble", [("pseudo", "shift"), ("sobol", "xor"), ("sobol", "shift")])
 def test_tensor_core_lowering(engine, rng, scramble):
-    """Correlated GBM baskets lower to tcgen05 (3 TF32 MMAs per 8 Wiener
+    """Correlated GBM baskets lower to tcgen05 (3 FP16 MMAs per 16 Wiener
     indices, 128 paths per CTA); other universes keep the CUDA-core kernel."""
     from bench import basket_equations
-    eqs, payoff, _, _ = basket_equations(12)
+    eqs, payoff, _, _ = basket_equations(20)
     p = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=rng, scramble=scramble, tensor_cores=True)
     assert p.uses_tensor_cores
     src = p.source
-    assert "_tc(const sde_args a)" in src and "__launch_bounds__(128)" in src
-    # K padded to 16 = 2 chunks of 8, 3 MMAs each, per unrolled step
-    n_mma = src.count("sde_mma_tf32(")
-    assert n_mma > 0 and n_mma % 6 == 0 and n_mma == 6 * src.count("sde_mma_commit(")
-    assert "sde_idesc_tf32(128, 16)" in src               # N = 12 processes padded to 16
+    assert "_tc(const sde_args a)" in src and "__launch_bounds__(128, 4)" in src
+    # K = 20 padded to 32 = 2 chunks of 16, 3 MMAs each, per unrolled step
+    n_mma = src.count("sde_mma_f16(")
+    assert n_mma > 0 and n_mma == 6 * src.count("sde_mma_commit(")
+    assert "sde_idesc_f16(128, 32)" in src                # N = 20 processes padded to 32
     assert "sde_mbar_wait_bounded" in src and "sde_tmem_dealloc" in src
+    # the B image: rows of K = diag(sigma) L scaled by 2^e (largest entry in
+    # [2^12, 2^13)), FP16 hi + lo, in the K-major core-matrix layout
+    _, _, sigma, L = basket_equations(20)
+    words = re.search(r"_kmat\[(\d+)\] = \{([^}]*)\}", src)
+    img = np.array([int(w, 16) for w in words.group(2).replace(",", " ").split()], dtype=np.uint16)
+    NP, KP = 32, 32
+    assert int(words.group(1)) == img.size == 2 * NP * KP
+    half = img.view(np.float16).astype(np.float64)
+    n, k = np.meshgrid(np.arange(NP), np.arange(KP), indexing="ij")
+    at = (n // 8) * (8 * KP) + (k // 8) * 64 + (n % 8) * 8 + k % 8
+    hi, lo = half[at], half[NP * KP + at]
+    K = np.zeros((NP, KP))
+    K[:20, :20] = L * sigma[:, None]
+    e = np.array([13 - np.frexp(np.abs(r).max())[1] if np.abs(r).max() > 0 else 0 for r in K])
+    kf = (K * np.ldexp(1.0, e)[:, None]).astype(np.float32)
+    assert np.array_equal(hi, kf.astype(np.float16).astype(np.float64))
+    assert np.array_equal(lo, (kf - kf.astype(np.float16).astype(np.float32)).astype(np.float16).astype(np.float64))
+    assert np.all(np.abs(hi[:20]).max(axis=1) < 2 ** 13) and np.all(np.abs(hi[:20]).max(axis=1) >= 2 ** 12)
     # a coefficient of 1 * X and a folded constant are eligible too
     q = engine.Plan(["dA = (0.01 * A) * dt + A * dW1 + ((0.5 * 0.2) * A) * dW2",
                      "dB = (0.3 * B) * dW2"], payoffs=["A + B"], precision="fp32", tensor_cores=True)

@@ -1,8 +1,9 @@
 """tcgen05 lowering of correlated GBM baskets (every dW coefficient is a
 constant times its own process).  The tensor-core kernel draws the same
 increments as the CUDA-core FP32 kernel and differs from it only by the
-3xTF32 product's rounding; against the FP64 oracle it meets the bar of the
-other FP32 kernels."""
+rounding of its product (three FP16 products of hi / lo splits, FP32
+accumulation); against the FP64 oracle it meets the bar of the other FP32
+kernels."""
 import math
 
 import numpy as np
@@ -36,7 +37,7 @@ def test_tensor_core_paths_match_cuda_core_kernel(engine, dim, rng):
     assert va.shape == vb.shape == (reps, n, len(times), dim)
     assert np.all(np.isfinite(va))
     rel = np.abs(va - vb) / np.abs(vb)
-    # 3xTF32 keeps about FP32 accuracy per step; 32 steps of GBM
+    # the split product keeps about FP32 accuracy per step; 32 steps of GBM
     assert rel.max() < 2e-5, np.percentile(rel, [50, 99, 100])
     sa, qa = a.estimates()
     sb, qb = b.estimates()
