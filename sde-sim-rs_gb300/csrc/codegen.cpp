@@ -323,8 +323,11 @@ struct Gen {
                 // dimension t*NI + k = group base (a multiple of 32) + e
                 const int e = g * NI + k, c = e / 32, l = e % 32;
                 if (!block_done[c]) {
-                    o.l(V("hv", c) + " = " + (mma ? "sde_sobol_hi_unrolled" : "sde_sobol_hi") +
-                        "(a.sobol_vt, mask_rep, a.sobol_dims, chunk0 + " + S(c) + ", " + V("H") + ", lane);");
+                    if (mma)  // fetched one group ahead (hv_prefetch)
+                        o.l(V("hv", c) + " = " + V("hvn", c) + ";");
+                    else
+                        o.l(V("hv", c) + " = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, chunk0 + " + S(c) +
+                            ", " + V("H") + ", lane);");
                     block_done[c] = true;
                 }
                 o.l("const sde_u32 " + V("y", k) + " = __shfl_sync(0xffffffffu, " + V("hv", c) + ", " + S(l) +
@@ -622,12 +625,16 @@ struct Gen {
         }
         o.l("  sde_mma_commit(MBAR);");
         o.l("}");
+        // while the MMA runs: the next group's Sobol high parts
+        if (xorm() && g == group() - 1) hv_prefetch(o, "chunk0 + " + S((group() * NI) / 32));
         o.l("tc_ok = sde_mbar_wait_bounded(MBAR, tc_phase) ? 1 : 0;");
         o.l("tc_phase ^= 1u;");
         o.l("__syncwarp();");
         o.l("sde_tc_fence_after();");
         o.l("float DM[" + S(NP) + "];");
-        for (int c = 0; c < NP / 16; ++c) o.l("sde_tmem_ld16_wait(TROW + " + S(c * 16) + "u, DM + " + S(c * 16) + ");");
+        // 16 columns per load: a block of D is consumed before the next one
+        // is loaded, so D and the state need not be live in full at once
+        for (int c = 0; c < NP; c += 16) o.l("sde_tmem_ld16_wait(TROW + " + S(c) + "u, DM + " + S(c) + ");");
         o.l("const float sdz = sdt * 0x1p-12f;");
         for (int p : u.levy) o.l(V("C", p) + " = " + V("X", p) + ";");
         poisson(o, "C", "tc");
@@ -816,9 +823,25 @@ struct Gen {
         o.l("(void)tc; (void)tn; (void)dt; (void)sdt;");
     }
 
+    // Sobol high parts of the 32-dimension chunks of the group starting at
+    // chunk `first` (an expression), for the tensor-core step's prefetch;
+    // chunks past the last step's dimensions are not read (the scramble-mask
+    // rows end there)
+    void hv_prefetch(Out& o, const std::string& first) const {
+        const int nb = (group() * NI) / 32;
+        for (int c = 0; c < nb; ++c)
+            o.l("if (32 * (" + first + " + " + S(c) + ") < n_steps * " + S(NI) + ") " + V("hvn", c) +
+                " = sde_sobol_hi_unrolled(a.sobol_vt, mask_rep, a.sobol_dims, " + first + " + " + S(c) + ", " +
+                V("H") + ", lane);");
+    }
+
     void time_loop(Out& o) {
         const int U = group();
         const int nblocks = uses_chacha() ? (U * NI) / 8 : (xorm() ? (U * NI) / 32 : 0);
+        if (mma && xorm()) {
+            for (int c = 0; c < nblocks; ++c) o.l("sde_u32 " + V("hvn", c) + " = 0u;");
+            hv_prefetch(o, "0");
+        }
         o.l("for (int t0 = 0; t0 < n_steps; t0 += " + S(U) + ") {");
         o.ind++;
         if (uses_chacha()) {
