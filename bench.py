@@ -459,7 +459,7 @@ def run_basket(args):
     # (the 64 x 64 diffusion product as three FP16 MMAs per 16 indices and
     # 128 paths, FP32 accumulation)
     legs = {}
-    for leg, tc in (("cuda_cores", False), ("tensor_cores", True)):
+    for leg, tc in (("cuda_cores", False), ("tensor_cores_row", "row"), ("tensor_cores", True)):
         if tc and args.cuda_cores_only:
             continue
         plan = sde_sim_rs.Plan(eqs, payoffs=[payoff], rng="sobol", scramble="xor", precision="fp32",

@@ -88,11 +88,15 @@ typedef struct sde_options {
  * constant times its own process (correlated GBM baskets), the step's
  * Wiener terms run as one tcgen05 product per 128 paths (three FP16
  * products of hi / lo splits, FP32 accumulation, about FP32 accuracy) and
- * the block size is 128.  Other plans keep the
- * CUDA-core kernel; sde_plan_tensor_cores tells which was built.
+ * 128 paths make one CTA.  With at least 32 processes and 32 Wiener
+ * indices, only dt and dW terms, and drifts that are constant * own
+ * process, two threads share a path (each draws half its normals and
+ * steps half its processes; 256 threads per CTA).  TC_ON_ROW keeps one
+ * thread per path.  Other plans keep the CUDA-core kernel;
+ * sde_plan_tensor_cores tells which was built.
  * No counterpart in the reference (its coefficient loop is
  * src/sim/euler.rs:17-33).                                                */
-enum { SDE_TC_OFF = 0, SDE_TC_ON = 1 };
+enum { SDE_TC_OFF = 0, SDE_TC_ON = 1, SDE_TC_ON_ROW = 2 };
 
 /* AS26: the reference's Abramowitz-Stegun 26.2.23 normal (|err| ~ 4.5e-4).
  * ACCURATE: that value refined by Halley steps on Phi through erfc of the

@@ -220,6 +220,21 @@ bool diffusion_matrix(const Universe& u, std::vector<std::vector<double>>& K) {
     return any;
 }
 
+// Every term of process p but its dW terms is (constant * X_p) * dt; c gets
+// the sum of those constants.
+bool linear_drift_of(const Universe& u, int p, double& c) {
+    c = 0.0;
+    for (const auto& t : u.procs[p].terms) {
+        if (t.kind == IncKind::Dw) continue;
+        ExprP k;
+        int q = -1;
+        double v = 0.0;
+        if (t.kind != IncKind::Dt || !split_linear_coef(t.coef, k, q) || q != p || !fold_const(k, v)) return false;
+        c += v;
+    }
+    return true;
+}
+
 enum class Mode { Forward, Batch };
 
 struct Gen {
@@ -589,9 +604,27 @@ struct Gen {
     // update in FP32 with d_p = D_p sqrt_dt 2^-(12 + e_p) = sum_j K_pj w_j.
     const MmaShape* mma = nullptr;
     std::vector<int> row_e;   // B row p is K_p * 2^row_e[p]
+
+    bool linear_drift(int p, double& c) const { return linear_drift_of(u, p, c); }
+
+    // With two threads per path (mma->split == 2), the thread of half h
+    // draws the normals of A columns [h KP/2, (h+1) KP/2), reads D columns
+    // [h NP/2, (h+1) NP/2) and steps those processes.
+    int half = 0;
+    int kcols() const { return mma->kpad / mma->split; }
+    int pcols() const { return mma->npad / mma->split; }
+    // 32-dimension Sobol chunks of a group that this thread's indices touch
+    std::vector<bool> own_chunks() const {
+        const int nb = (group() * NI) / 32;
+        std::vector<bool> need(std::max(1, nb), false);
+        for (int g = 0; g < group(); ++g)
+            for (int k = half * kcols(); k < std::min(NI, (half + 1) * kcols()); ++k) need[(g * NI + k) / 32] = true;
+        return need;
+    }
+
     void step_mma(Out& o, int g, std::vector<bool>& done) const {
-        const int KP = mma->kpad, NP = mma->npad;
-        for (int k8 = 0; k8 < KP; k8 += 8) {
+        const int KH = kcols(), PH = pcols();
+        for (int k8 = half * KH; k8 < (half + 1) * KH; k8 += 8) {
             if (k8 < NI) {
                 uniforms(o, g, done, k8, std::min(k8 + 8, NI));
                 wiener(o, xorm() && f32, "0x1p12f", k8, std::min(k8 + 8, NI));
@@ -612,37 +645,60 @@ struct Gen {
             o.l("  *(uint4*)(ARH + " + off + ") = make_uint4(h0, h1, h2, h3);");
             o.l("  *(uint4*)(ARL + " + off + ") = make_uint4(l0, l1, l2, l3); }");
         }
+        // A ready: every thread arrives after its writes; thread 0 waits for
+        // all of them, then issues the product and commits it to DBAR
         o.l("sde_fence_async_smem();");
         o.l("sde_tc_fence_before();");
-        o.l("if (!__syncthreads_and(tc_ok)) { tc_fail = 1; break; }");
-        o.l("sde_tc_fence_after();");
-        o.l("if (threadIdx.x == 0) {");
-        for (int c = 0; c < KP / 16; ++c) {
-            const std::string dc = S(c * 16) + "ull";  // 256 bytes further along K, in 16-byte units
-            o.l("  sde_mma_f16(tmem, ADH + " + dc + ", BDH + " + dc + ", IDESC, " + (c ? "1u" : "0u") + ");");
-            o.l("  sde_mma_f16(tmem, ADH + " + dc + ", BDL + " + dc + ", IDESC, 1u);");
-            o.l("  sde_mma_f16(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
+        o.l("sde_mbar_arrive(ABAR);");
+        if (half == 0) {
+            // the whole of warp 0 waits, so lane 0 never waits behind lanes
+            // of its own warp suspended on DBAR
+            o.l("if (threadIdx.x < 32) {");
+            o.l("  const bool a_ready = sde_mbar_wait_bounded(ABAR, tc_phase);");
+            o.l("  if (!a_ready) tc_ok = 0;");
+            o.l("  if (threadIdx.x == 0 && a_ready) {");
+            o.l("    sde_tc_fence_after();");
+            for (int c = 0; c < mma->kpad / 16; ++c) {
+                const std::string dc = S(c * 16) + "ull";  // 256 bytes further along K, in 16-byte units
+                o.l("    sde_mma_f16(tmem, ADH + " + dc + ", BDH + " + dc + ", IDESC, " + (c ? "1u" : "0u") + ");");
+                o.l("    sde_mma_f16(tmem, ADH + " + dc + ", BDL + " + dc + ", IDESC, 1u);");
+                o.l("    sde_mma_f16(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
+            }
+            o.l("    sde_mma_commit(DBAR);");
+            o.l("  }");
+            o.l("  __syncwarp();");
+            o.l("}");
         }
-        o.l("  sde_mma_commit(MBAR);");
-        o.l("}");
         // while the MMA runs: the next group's Sobol high parts
         if (xorm() && g == group() - 1) hv_prefetch(o, "chunk0 + " + S((group() * NI) / 32));
-        o.l("tc_ok = sde_mbar_wait_bounded(MBAR, tc_phase) ? 1 : 0;");
+        o.l("if (!sde_mbar_wait_bounded(DBAR, tc_phase)) tc_ok = 0;");
         o.l("tc_phase ^= 1u;");
-        o.l("__syncwarp();");
+        // a warp leaves together (tcgen05.ld below is warp-collective)
+        o.l("if (!__all_sync(0xffffffffu, tc_ok)) break;");
         o.l("sde_tc_fence_after();");
-        o.l("float DM[" + S(NP) + "];");
+        o.l("float DM[" + S(PH) + "];");
         // 16 columns per load: a block of D is consumed before the next one
         // is loaded, so D and the state need not be live in full at once
-        for (int c = 0; c < NP; c += 16) o.l("sde_tmem_ld16_wait(TROW + " + S(c) + "u, DM + " + S(c) + ");");
+        for (int c = 0; c < PH; c += 16) o.l("sde_tmem_ld16_wait(TROW + " + S(c) + "u, DM + " + S(c) + ");");
         o.l("const float sdz = sdt * 0x1p-12f;");
-        for (int p : u.levy) o.l(V("C", p) + " = " + V("X", p) + ";");
+        for (int p : u.levy)
+            if (p >= plo && p < pend()) o.l(V("C", p) + " = " + V("X", p) + ";");
         poisson(o, "C", "tc");
         for (int p : u.levy) {
+            if (p < plo || p >= pend()) continue;
+            const std::string d = "DM[" + S(p - half * PH) + "]";
             const std::string f = row_e[p] == 0 ? "sdz" : "(sdz * " + lit(std::ldexp(1.0, -row_e[p]), true) + ")";
-            euler_update(o, p, "C", "DM[" + S(p) + "] * " + f);
+            double c = 0.0;
+            // N = X + X (c dt + d): two FMAs (c dt is shared by equal c).  Not
+            // X (1 + c dt + d): 1 + c dt would round the same way every step
+            // and bias the paths coherently
+            if (linear_drift(p, c))
+                o.l("const float " + V("N", p) + " = fmaf(" + V("X", p) + ", fmaf(" + d + ", " + f + ", " + lit(c, true) +
+                    " * dt), " + V("X", p) + ");");
+            else
+                euler_update(o, p, "C", d + " * " + f);
         }
-        for (int p = 0; p < P; ++p) o.l(V("X", p) + " = " + V("N", p) + ";");
+        for (int p = plo; p < pend(); ++p) o.l(V("X", p) + " = " + V("N", p) + ";");
     }
 
     // Forward kernel on the tensor cores (one path per thread, 128 paths per
@@ -692,7 +748,8 @@ struct Gen {
             o.l(row);
         }
         o.l("};");
-        o.l("extern \"C\" __global__ void __launch_bounds__(128, " + S(mma->min_blocks) + ") " + name +
+        const int TH = 128 * mma->split;  // threads per CTA
+        o.l("extern \"C\" __global__ void __launch_bounds__(" + S(TH) + ", " + S(mma->min_blocks) + ") " + name +
             "(const sde_args a) {");
         o.ind++;
         o.l("extern __shared__ __align__(1024) unsigned char sde_smem[];");
@@ -701,12 +758,14 @@ struct Gen {
         o.l("unsigned char* const SBH = SAL + " + S(128 * KP * 2) + ";");
         o.l("unsigned char* const SBL = SBH + " + S(NP * KP * 2) + ";");
         o.l("sde_u64* const MBP = (sde_u64*)(SBL + " + S(NP * KP * 2) + ");");
-        o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 1);");
-        o.l("const sde_u32 MBAR = sde_smem_addr(MBP);");
-        o.l("for (int e = threadIdx.x; e < " + S(2 * 128 * KP * 2 / 16) + "; e += 128) ((uint4*)SAH)[e] = make_uint4(0u, 0u, 0u, 0u);");
-        o.l("for (int e = threadIdx.x; e < " + S(2 * NP * KP * 2 / 16) + "; e += 128) ((uint4*)SBH)[e] = ((const uint4*)" +
-            name + "_kmat)[e];");
-        o.l("if (threadIdx.x == 0) { sde_mbar_init(MBAR, 1u); sde_fence_mbar_init(); }");
+        o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 2);");
+        // ABAR: A written (every thread arrives); DBAR: product committed
+        o.l("const sde_u32 ABAR = sde_smem_addr(MBP), DBAR = sde_smem_addr(MBP + 1);");
+        o.l("for (int e = threadIdx.x; e < " + S(2 * 128 * KP * 2 / 16) + "; e += " + S(TH) +
+            ") ((uint4*)SAH)[e] = make_uint4(0u, 0u, 0u, 0u);");
+        o.l("for (int e = threadIdx.x; e < " + S(2 * NP * KP * 2 / 16) + "; e += " + S(TH) +
+            ") ((uint4*)SBH)[e] = ((const uint4*)" + name + "_kmat)[e];");
+        o.l("if (threadIdx.x == 0) { sde_mbar_init(ABAR, " + S(TH) + "u); sde_mbar_init(DBAR, 1u); sde_fence_mbar_init(); }");
         o.l("__syncwarp();");
         o.l("if (threadIdx.x < 32) sde_tmem_alloc(sde_smem_addr(TSLOT), " + S(mma->ncols) + "u);");
         o.l("sde_fence_async_smem();");
@@ -714,38 +773,82 @@ struct Gen {
         o.l("__syncthreads();");
         o.l("sde_tc_fence_after();");
         o.l("const sde_u32 tmem = *TSLOT;");
-        o.l("const sde_u32 TROW = tmem + ((sde_u32)(threadIdx.x & ~31u) << 16);");
+        // the thread's path in the tile (its A row and TMEM lane) and half
+        o.l("const int r = threadIdx.x & 127;");
+        o.l("const int half = threadIdx.x >> 7;");
+        o.l("(void)half;");
+        // warps w and w + 4 reach lanes 32 (w % 4) ..; half h reads D columns from h NP / split
+        o.l("const sde_u32 TROW = tmem + ((sde_u32)(r & ~31) << 16) + (sde_u32)half * " + S(pcols()) + "u;");
         // LBO: the two core matrices of one MMA's K slice; SBO: 8-row groups
         o.l("const sde_u32 IDESC = sde_idesc_f16(128, " + S(NP) + ");");
         o.l("const sde_u64 ADH = sde_smem_desc(sde_smem_addr(SAH), 128u, " + S(KP * 16) + "u);");
         o.l("const sde_u64 ADL = sde_smem_desc(sde_smem_addr(SAL), 128u, " + S(KP * 16) + "u);");
         o.l("const sde_u64 BDH = sde_smem_desc(sde_smem_addr(SBH), 128u, " + S(KP * 16) + "u);");
         o.l("const sde_u64 BDL = sde_smem_desc(sde_smem_addr(SBL), 128u, " + S(KP * 16) + "u);");
-        o.l("unsigned char* const ARH = SAH + (threadIdx.x >> 3) * " + S(16 * KP) + " + (threadIdx.x & 7) * 16;");
+        o.l("(void)ADH; (void)ADL; (void)BDH; (void)BDL; (void)IDESC;");
+        o.l("unsigned char* const ARH = SAH + (r >> 3) * " + S(16 * KP) + " + (r & 7) * 16;");
         o.l("unsigned char* const ARL = ARH + " + S(128 * KP * 2) + ";");
-        o.l("int tc_ok = 1, tc_fail = 0;");
+        o.l("int tc_ok = 1;");
         o.l("sde_u32 tc_phase = 0u;");
-        o.l("(void)tc_fail;");
+        row = "r";
+        cta = "128";
         shared_prologue(o);
-        lane_prologue(o);
-        store(o, "0");
-        time_loop(o);
-        // teardown: every thread arrives here (the break above is block-uniform)
+        if (mma->split == 1) {
+            lane_prologue(o);
+            store(o, "0");
+            time_loop(o);
+        } else {
+            // each half steps its own processes in its own copy of the loop
+            // (its registers hold only those); the halves meet only at the
+            // mbarriers, whose waits are bounded
+            for (int h = 0; h < 2; ++h) {
+                half = h;
+                plo = h * pcols();
+                phi = std::min(P, (h + 1) * pcols());
+                o.l(h == 0 ? "if (half == 0) {" : "} else {");
+                o.ind++;
+                lane_prologue(o);
+                store(o, "0");
+                time_loop(o);
+                // the state goes to shared memory (the operand area, free
+                // now) for the payoffs
+                for (int p = plo; p < pend(); ++p) o.l("((float*)sde_smem)[" + S(p * 128) + " + r] = " + V("X", p) + ";");
+                o.ind--;
+            }
+            o.l("}");
+            half = 0;
+            plo = 0;
+            phi = -1;
+        }
+        // teardown: every thread arrives here; the loops above hold no
+        // CTA-wide barrier
         o.l("sde_tc_fence_before();");
         o.l("const int tc_all = __syncthreads_and(tc_ok);");
         o.l("sde_tc_fence_after();");
         o.l("if (threadIdx.x < 32) {");
-        o.l("  if (!tc_all) (void)sde_mbar_wait_bounded(MBAR, tc_phase ^ 1u);");
+        o.l("  if (!tc_all) (void)sde_mbar_wait_bounded(DBAR, tc_phase ^ 1u);");
         o.l("  __syncwarp();");
         o.l("  sde_tmem_dealloc(tmem, " + S(mma->ncols) + "u);");
         o.l("}");
         o.l("if (!tc_all && threadIdx.x == 0 && a.status) atomicOr(a.status, 1);");
         if (NPAY > 0) {
             o.l("double fs[" + S(NPAY) + "] = {}, fq[" + S(NPAY) + "] = {};");
-            payoffs(o, NPAY);
+            if (mma->split == 1) {
+                payoffs(o, NPAY);
+            } else {
+                o.l("if (half == 0) {");
+                o.ind++;
+                o.l("const bool active = base + r < a.n_paths;");
+                for (int p = 0; p < P; ++p) o.l("const float X" + S(p) + " = ((const float*)sde_smem)[" + S(p * 128) + " + r];");
+                payoffs(o, NPAY);
+                o.ind--;
+                o.l("}");
+            }
             o.l("sde_block_reduce_store<" + S(NPAY) + ">(fs, fq, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " +
                 S(NPAY) + "u) * 4u);");
         }
+        row = "threadIdx.x";
+        cta = "blockDim.x";
         o.ind--;
         o.l("}");
         return o.s.str();
@@ -756,19 +859,26 @@ struct Gen {
         o.l("{ const int slot = __ldg(&a.out_tidx[" + tidx + "]);");
         o.l("  if (slot >= 0 && " + V("active") + ") {");
         o.l("    " + R + "* dst = OUT + ((sde_u64)rep * a.n_out + slot) * (sde_u64)" + S(P) + " * a.n_paths + " + V("i") + ";");
-        for (int p = 0; p < P; ++p)
+        for (int p = plo; p < pend(); ++p)
             o.l("    dst[(sde_u64)" + S(p) + " * a.n_paths] = " + V("X", p) + ";");
         o.l("  } }");
     }
+
+    // Processes [plo, pend()) are this thread's (all but in the tensor-core
+    // kernel with two threads per path); `row` is the thread's path within
+    // the CTA and `cta` the CTA's paths per lane.
+    int plo = 0, phi = -1;
+    int pend() const { return phi < 0 ? P : phi; }
+    std::string row = "threadIdx.x", cta = "blockDim.x";
 
     // ---- per-lane state --------------------------------------------------
     void lane_prologue(Out& o) const {
         if (mode == Mode::Forward) {
             o.l("const sde_u64 " + V("i") + " = base + " + S(0) + "ull + (sde_u64)" + (sfx.empty() ? "0" : sfx.substr(1)) +
-                " * blockDim.x + threadIdx.x;");
+                " * " + cta + " + " + row + ";");
             o.l("const bool " + V("active") + " = " + V("i") + " < a.n_paths;");
             o.l("const sde_u64 " + V("scen") + " = a.path_base + (sde_u64)rep * a.n_paths + " + V("i") + ";");
-            for (int p = 0; p < P; ++p) o.l(R + " " + V("X", p) + " = (" + R + ")__ldg(&a.x0[" + S(p) + "]);");
+            for (int p = plo; p < pend(); ++p) o.l(R + " " + V("X", p) + " = (" + R + ")__ldg(&a.x0[" + S(p) + "]);");
         } else {
             o.l("const sde_u64 " + V("i") + " = first + (sde_u64)" + (sfx.empty() ? "0" : sfx.substr(1)) +
                 " * blockDim.x + threadIdx.x;");
@@ -777,7 +887,7 @@ struct Gen {
             for (int p = 0; p < P; ++p) o.l(R + " " + V("X", p) + " = (" + R + ")__ldg(&a.x0[in.x0_off + " + S(p) + "]);");
         }
         o.l("(void)" + V("scen") + ";");
-        for (int p = 0; p < P; ++p) o.l(R + " " + V("C", p) + " = " + V("X", p) + ";");
+        for (int p = plo; p < pend(); ++p) o.l(R + " " + V("C", p) + " = " + V("X", p) + ";");
         const std::string seed = mode == Mode::Forward ? "a.seed" : "in.seed";
         if (uses_chacha()) o.l("sde_u32 " + V("key") + "[8]; sde_seed_from_u64(" + seed + " + " + V("scen") + ", " + V("key") + ");");
         if (shiftm()) o.l("const sde_u32 " + V("G") + " = sde_gray((sde_u32)(" + V("scen") + " + 5ull));");
@@ -793,7 +903,7 @@ struct Gen {
         o.l("(void)lane;");
         if (mode == Mode::Forward) {
             o.l("const int rep = blockIdx.y;");
-            o.l("const sde_u64 base = (sde_u64)blockIdx.x * blockDim.x * " + S(ppt) + "ull;");
+            o.l("const sde_u64 base = (sde_u64)blockIdx.x * " + cta + " * " + S(ppt) + "ull;");
             o.l("const int n_steps = a.T - 1;");
             for (int k = 0; k < (int)u.params.size(); ++k)
                 o.l("const " + R + " PR" + S(k) + " = (" + R + ")__ldg(&a.params[" + S(k) + "]);");
@@ -828,9 +938,10 @@ struct Gen {
     // chunks past the last step's dimensions are not read (the scramble-mask
     // rows end there)
     void hv_prefetch(Out& o, const std::string& first) const {
-        const int nb = (group() * NI) / 32;
-        for (int c = 0; c < nb; ++c)
-            o.l("if (32 * (" + first + " + " + S(c) + ") < n_steps * " + S(NI) + ") " + V("hvn", c) +
+        const std::vector<bool> need = own_chunks();
+        for (int c = 0; c < (int)need.size(); ++c)
+            if (need[c])
+                o.l("if (32 * (" + first + " + " + S(c) + ") < n_steps * " + S(NI) + ") " + V("hvn", c) +
                 " = sde_sobol_hi_unrolled(a.sobol_vt, mask_rep, a.sobol_dims, " + first + " + " + S(c) + ", " +
                 V("H") + ", lane);");
     }
@@ -839,7 +950,9 @@ struct Gen {
         const int U = group();
         const int nblocks = uses_chacha() ? (U * NI) / 8 : (xorm() ? (U * NI) / 32 : 0);
         if (mma && xorm()) {
-            for (int c = 0; c < nblocks; ++c) o.l("sde_u32 " + V("hvn", c) + " = 0u;");
+            const std::vector<bool> need = own_chunks();
+            for (int c = 0; c < nblocks; ++c)
+                if (need[c]) o.l("sde_u32 " + V("hvn", c) + " = 0u;");
             hv_prefetch(o, "0");
         }
         o.l("for (int t0 = 0; t0 < n_steps; t0 += " + S(U) + ") {");
@@ -1099,21 +1212,38 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
     if (s.precision != PREC_FP32 || s.scheme != SCHEME_EULER || s.adjoint || s.ppt != 1 || !u.alg.empty()) return m;
     std::vector<std::vector<double>> K;
     if (!diffusion_matrix(u, K)) return m;
-    m.npad = std::max(16, (u.n_processes() + 15) / 16 * 16);   // M = 128 takes N = 16..256 in steps of 16
-    m.kpad = std::max(16, (u.n_stochastic() + 15) / 16 * 16);  // K = 16 per FP16 MMA
+    const int P = u.n_processes(), NI = u.n_stochastic();
+    // two threads per path for wide universes whose drifts are linear in
+    // their own process (each thread then needs only its half of the state)
+    bool two = s.tensor_cores == 1 && P >= 32 && NI >= 32;
+    for (int p = 0; two && p < P; ++p) {
+        double c = 0.0;
+        two = linear_drift_of(u, p, c);
+    }
+    for (int k = 0; two && k < NI; ++k) two = u.token_kind[k] == IncKind::Dw;
+    m.split = two ? 2 : 1;
+    const int nq = 16 * m.split;                            // each half's columns: multiples of 16
+    m.npad = std::max(nq, (P + nq - 1) / nq * nq);          // M = 128 takes N = 16..256 in steps of 16
+    m.kpad = std::max(nq, (NI + nq - 1) / nq * nq);         // K = 16 per FP16 MMA
     if (m.npad > 256) return m;
     m.ncols = 32;
     while (m.ncols < m.npad) m.ncols *= 2;
-    const int need = 2 * 128 * m.kpad * 2 + 2 * m.npad * m.kpad * 2 + 16;
+    const int operands = 2 * 128 * m.kpad * 2 + 2 * m.npad * m.kpad * 2;
+    if (m.split == 2 && 128 * P * 4 > operands) {            // the payoff exchange reuses the operand area
+        m.split = 1;
+        return mma_shape(u, [&] { KernelSpec t = s; t.tensor_cores = 2; return t; }());
+    }
+    const int need = operands + 32;                          // + two mbarriers and the TMEM address
     // at most 512 / ncols CTAs of an SM can hold tensor memory at once: ask
     // for enough shared memory (228 KB per SM) that no more are resident
     const int floor_bytes = 233472 / (512 / m.ncols + 1) + 1;
     m.smem_bytes = std::max(need, floor_bytes);
     if (m.smem_bytes > 227 * 1024) return m;
     // CTAs per SM that the shared memory allows (1 KB reserved and 1 KB of
-    // static reduction scratch each), capped at 4: the register budget of
-    // __launch_bounds__
-    m.min_blocks = std::max(1, std::min(4, 233472 / (m.smem_bytes + 2048)));
+    // static reduction scratch each), capped by the register budget of
+    // __launch_bounds__: 128 registers a thread (one thread per path) or 85
+    // (two threads per path, 3 CTAs of 256)
+    m.min_blocks = std::max(1, std::min(m.split == 2 ? 3 : 4, 233472 / (m.smem_bytes + 2048)));
     m.eligible = true;
     return m;
 }
@@ -1127,7 +1257,7 @@ std::string generate_source(const Universe& u, const KernelSpec& s) {
     if (s.tensor_cores) {
         const MmaShape m = mma_shape(u, s);
         std::vector<std::vector<double>> K;
-        if (!m.eligible || !diffusion_matrix(u, K) || s.block != 128)
+        if (!m.eligible || !diffusion_matrix(u, K) || s.block != 128 * m.split)
             throw std::runtime_error("the universe is not eligible for the tensor-core lowering");
         g.mma = &m;
         src += g.forward_mma(forward_kernel_name(s), K);

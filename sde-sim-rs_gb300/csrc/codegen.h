@@ -26,6 +26,7 @@ struct KernelSpec {
     int ppt = 1;                        // paths per thread (independent chains)
     int icdf = 0;                       // 0: AS 26.2.23 (reference), 1: accurate
     int tensor_cores = 0;               // 1: correlated diffusions on tcgen05 when eligible
+                                        // 2: the same with one thread per path always
     // adjoint: parameters and initial values to differentiate
     bool adjoint = false;
     std::vector<int> grad_params;       // parameter indices
@@ -44,6 +45,7 @@ struct MmaShape {
     int ncols = 0;        // tensor-memory columns allocated (power of 2 >= 32)
     int smem_bytes = 0;   // dynamic shared memory of the kernel
     int min_blocks = 1;   // CTAs per SM the kernel is register-budgeted for
+    int split = 1;        // threads per path (2: each steps half the processes)
 };
 MmaShape mma_shape(const Universe& u, const KernelSpec& s);
 

@@ -361,12 +361,15 @@ SDE_DEV void sde_tmem_dealloc(sde_u32 taddr, sde_u32 ncols) {
 SDE_DEV void sde_mbar_init(sde_u32 mbar, sde_u32 count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
+/* suspends the thread until the phase completes or about 10 us pass (the
+ * suspend-time hint, in ns), instead of returning at once: waiting warps
+ * then take no issue slots from the other warps of the SM */
 SDE_DEV bool sde_mbar_try_wait(sde_u32 mbar, sde_u32 parity) {
     sde_u32 ok;
     asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3; selp.u32 %0, 1, 0, p; }"
         : "=r"(ok)
-        : "r"(mbar), "r"(parity)
+        : "r"(mbar), "r"(parity), "r"(10000u)
         : "memory");
     return ok != 0u;
 }
@@ -376,6 +379,10 @@ SDE_DEV bool sde_mbar_wait_bounded(sde_u32 mbar, sde_u32 parity) {
     while (!sde_mbar_try_wait(mbar, parity))
         if (clock64() - t0 > 2000000000ll) return false;
     return true;
+}
+/* one arrival (release) on a CTA mbarrier */
+SDE_DEV void sde_mbar_arrive(sde_u32 mbar) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(mbar) : "memory");
 }
 SDE_DEV void sde_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 SDE_DEV void sde_tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }

@@ -389,7 +389,8 @@ static KernelSpec spec_from(const sde_options* o) {
     s.icdf = o->icdf;
     if (s.icdf != SDE_ICDF_AS26 && s.icdf != SDE_ICDF_ACCURATE) fail(SDE_ERR_INVALID, "unknown icdf");
     s.tensor_cores = o->tensor_cores;
-    if (s.tensor_cores != SDE_TC_OFF && s.tensor_cores != SDE_TC_ON) fail(SDE_ERR_INVALID, "unknown tensor_cores");
+    if (s.tensor_cores != SDE_TC_OFF && s.tensor_cores != SDE_TC_ON && s.tensor_cores != SDE_TC_ON_ROW)
+        fail(SDE_ERR_INVALID, "unknown tensor_cores");
     if (s.ppt != 1 && s.ppt != 2 && s.ppt != 4) fail(SDE_ERR_INVALID, "paths_per_thread must be 1, 2 or 4");
     if (s.ckpt_every > 256) fail(SDE_ERR_INVALID, "ckpt_every must be at most 256");
     return s;
@@ -429,7 +430,7 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
         // kernel otherwise
         const MmaShape m = mma_shape(p->u, p->spec);
         if (m.eligible) {
-            p->spec.block = 128;  // one MMA row per thread
+            p->spec.block = 128 * m.split;  // one MMA row per path, one or two threads per path
             p->auto_block = false;
             p->mma_smem = m.smem_bytes;
         } else {
@@ -478,7 +479,9 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         const uint64_t wpb = std::min<uint64_t>(8, std::max<uint64_t>(1, (warps + sms - 1) / std::max(1, sms)));
         block = (int)(32 * wpb);
     }
-    const uint64_t per_block = (uint64_t)block * ppt_eff;
+    // a tensor-core CTA steps 128 paths (one MMA tile) with 128 or 256 threads
+    const bool tc_plan = p->spec.tensor_cores && !p->spec.adjoint;
+    const uint64_t per_block = tc_plan ? 128ull : (uint64_t)block * ppt_eff;
     const uint64_t gx = (N + per_block - 1) / per_block;
     if (gx > 0x7fffffffull) fail(SDE_ERR_INVALID, "too many paths for one launch");
 
@@ -620,7 +623,7 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         A.ckpt = r->ckpt.as<float>();
     }
 
-    const bool tc = p->spec.tensor_cores && !p->spec.adjoint;
+    const bool tc = tc_plan;
     if (tc && N > 0) {
         r->status = DBuf(16);
         r->status_host = HBuf(16);

@@ -156,13 +156,14 @@ class Plan:
                  scramble: str = "shift", precision: str = "fp64", semantics: str = "reference",
                  output: str = "full", block_size: int = 0, grad_params: Sequence[str] | None = None,
                  grad_x0: Sequence[str] | None = None, ckpt_every: int = 0, paths_per_thread: int = 1,
-                 icdf: str = "as26", tensor_cores: bool = False):
+                 icdf: str = "as26", tensor_cores: bool | str = False):
         """grad_params / grad_x0 make an adjoint plan: each run also returns
         the pathwise derivatives of E[payoffs[0]] with respect to those
         parameters and initial values (Euler-Maruyama, checkpoints every
         ckpt_every steps, default 19).  tensor_cores=True lowers the dW
         terms of an FP32 Euler universe whose diffusions are constant * own
-        process (correlated GBM) to one tcgen05 product per 128 paths;
+        process (correlated GBM) to one tcgen05 product per 128 paths, with
+        two threads per path for wide universes ("row": always one);
         ``uses_tensor_cores`` says whether the universe was eligible."""
         if scheme not in N.SCHEME:
             raise ValueError(f"unknown scheme '{scheme}'")
@@ -178,7 +179,9 @@ class Plan:
         opts.ckpt_every = ckpt_every
         opts.paths_per_thread = paths_per_thread
         opts.icdf = N.ICDF[icdf]
-        opts.tensor_cores = 1 if tensor_cores else 0
+        if tensor_cores not in N.TENSOR_CORES:
+            raise ValueError(f"unknown tensor_cores {tensor_cores!r}")
+        opts.tensor_cores = N.TENSOR_CORES[tensor_cores]
         self.equations = list(equations)
         self.params = list(params)
         self.payoffs = list(payoffs)

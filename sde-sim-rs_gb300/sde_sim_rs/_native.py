@@ -28,6 +28,7 @@ PRECISION = {"fp64": 0, "fp32": 1}
 SEMANTICS = {"reference": 0, "textbook": 1}
 OUTPUT = {"full": 0, "checkpoints": 1, "terminal": 2, "none": 3}
 ICDF = {"as26": 0, "reference": 0, "accurate": 1}
+TENSOR_CORES = {False: 0, True: 1, "off": 0, "auto": 1, "row": 2}
 LAYOUT_REFERENCE, LAYOUT_DEVICE = 0, 1
 
 

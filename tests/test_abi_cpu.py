@@ -207,6 +207,18 @@ def test_tensor_core_lowering(engine, rng, scramble):
     assert np.array_equal(hi, kf.astype(np.float16).astype(np.float64))
     assert np.array_equal(lo, (kf - kf.astype(np.float16).astype(np.float32)).astype(np.float16).astype(np.float64))
     assert np.all(np.abs(hi[:20]).max(axis=1) < 2 ** 13) and np.all(np.abs(hi[:20]).max(axis=1) >= 2 ** 12)
+    # two threads per path from 32 processes and 32 indices with linear drifts
+    eqs32, pay32, _, _ = basket_equations(32)
+    assert "__launch_bounds__(256, 3)" in engine.Plan(eqs32, payoffs=[pay32], precision="fp32",
+                                                      tensor_cores=True).source
+    assert "__launch_bounds__(128, 4)" in engine.Plan(eqs32, payoffs=[pay32], precision="fp32",
+                                                      tensor_cores="row").source
+    cross = list(eqs32)
+    cross[0] = cross[0].replace("(0.02 * S1) * dt", "(0.02 * S2) * dt")
+    q = engine.Plan(cross, payoffs=[pay32], precision="fp32", tensor_cores=True)
+    assert q.uses_tensor_cores and "__launch_bounds__(128, 4)" in q.source
+    with pytest.raises(ValueError):
+        engine.Plan(eqs32, precision="fp32", tensor_cores="sometimes")
     # a coefficient of 1 * X and a folded constant are eligible too
     q = engine.Plan(["dA = (0.01 * A) * dt + A * dW1 + ((0.5 * 0.2) * A) * dW2",
                      "dB = (0.3 * B) * dW2"], payoffs=["A + B"], precision="fp32", tensor_cores=True)

@@ -21,14 +21,17 @@ def _init(dim):
     return {f"S{i + 1}": 100.0 for i in range(dim)}
 
 
-@pytest.mark.parametrize("dim", [4, 20, 64])
+@pytest.mark.parametrize("dim,layout", [(4, "auto"), (20, "auto"), (64, "auto"), (64, "row"), (40, "auto")])
 @pytest.mark.parametrize("rng", list(RNGS))
-def test_tensor_core_paths_match_cuda_core_kernel(engine, dim, rng):
+def test_tensor_core_paths_match_cuda_core_kernel(engine, dim, layout, rng):
+    """4 and 20 dimensions: one thread per path; 64 and 40: two threads per
+    path ("row" forces one); 40 pads N and K to 64 with a half-empty second
+    half."""
     eqs, payoff, _, _ = basket_equations(dim)
     r, s = RNGS[rng]
     times = np.linspace(0.0, 1.0, 33)
     n, reps = 1000, 2  # 1000 = 7 full CTAs of 128 paths and a ragged one
-    tc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=r, scramble=s, tensor_cores=True)
+    tc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=r, scramble=s, tensor_cores=layout)
     cc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=r, scramble=s)
     assert tc.uses_tensor_cores and not cc.uses_tensor_cores
     a = tc.run(times, _init(dim), n, replicates=reps, seed=5)
