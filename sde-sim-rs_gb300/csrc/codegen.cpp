@@ -338,9 +338,8 @@ struct Gen {
                 // dimension t*NI + k = group base (a multiple of 32) + e
                 const int e = g * NI + k, c = e / 32, l = e % 32;
                 if (!block_done[c]) {
-                    if (mma)  // fetched one group ahead (hv_prefetch)
-                        o.l(V("hv", c) + " = " + V("hvn", c) + ";");
-                    else
+                    // forward kernels took it from the one-group-ahead fetch
+                    if (!hv_pf())
                         o.l(V("hv", c) + " = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, chunk0 + " + S(c) +
                             ", " + V("H") + ", lane);");
                     block_done[c] = true;
@@ -616,9 +615,10 @@ struct Gen {
     // 32-dimension Sobol chunks of a group that this thread's indices touch
     std::vector<bool> own_chunks() const {
         const int nb = (group() * NI) / 32;
+        const int k0 = mma ? half * kcols() : 0, k1 = mma ? std::min(NI, (half + 1) * kcols()) : NI;
         std::vector<bool> need(std::max(1, nb), false);
         for (int g = 0; g < group(); ++g)
-            for (int k = half * kcols(); k < std::min(NI, (half + 1) * kcols()); ++k) need[(g * NI + k) / 32] = true;
+            for (int k = k0; k < k1; ++k) need[(g * NI + k) / 32] = true;
         return need;
     }
 
@@ -645,36 +645,54 @@ struct Gen {
             o.l("  *(uint4*)(ARH + " + off + ") = make_uint4(h0, h1, h2, h3);");
             o.l("  *(uint4*)(ARL + " + off + ") = make_uint4(l0, l1, l2, l3); }");
         }
-        // A ready: every thread arrives after its writes; thread 0 waits for
-        // all of them, then issues the product and commits it to DBAR
+        // A ready: a CTA barrier whose vote also ends the loop together;
+        // then thread 0 issues the product and commits it to DBAR.
         o.l("sde_fence_async_smem();");
         o.l("sde_tc_fence_before();");
-        o.l("sde_mbar_arrive(ABAR);");
-        if (half == 0) {
-            // the whole of warp 0 waits, so lane 0 never waits behind lanes
-            // of its own warp suspended on DBAR
-            o.l("if (threadIdx.x < 32) {");
-            o.l("  const bool a_ready = sde_mbar_wait_bounded(ABAR, tc_phase);");
-            o.l("  if (!a_ready) tc_ok = 0;");
-            o.l("  if (threadIdx.x == 0 && a_ready) {");
-            o.l("    sde_tc_fence_after();");
+        auto issue = [&](const std::string& pad) {
             for (int c = 0; c < mma->kpad / 16; ++c) {
                 const std::string dc = S(c * 16) + "ull";  // 256 bytes further along K, in 16-byte units
-                o.l("    sde_mma_f16(tmem, ADH + " + dc + ", BDH + " + dc + ", IDESC, " + (c ? "1u" : "0u") + ");");
-                o.l("    sde_mma_f16(tmem, ADH + " + dc + ", BDL + " + dc + ", IDESC, 1u);");
-                o.l("    sde_mma_f16(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
+                o.l(pad + "sde_mma_f16(tmem, ADH + " + dc + ", BDH + " + dc + ", IDESC, " + (c ? "1u" : "0u") + ");");
+                o.l(pad + "sde_mma_f16(tmem, ADH + " + dc + ", BDL + " + dc + ", IDESC, 1u);");
+                o.l(pad + "sde_mma_f16(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
             }
-            o.l("    sde_mma_commit(DBAR);");
-            o.l("  }");
-            o.l("  __syncwarp();");
+            o.l(pad + "sde_mma_commit(DBAR);");
+        };
+        if (mma->split == 1) {
+            // one thread per path: a CTA vote, the loop's only exit, so every
+            // warp takes the same votes
+            o.l("if (!__syncthreads_and(tc_ok)) break;");
+            o.l("sde_tc_fence_after();");
+            o.l("if (threadIdx.x == 0) {");
+            issue("  ");
             o.l("}");
+        } else {
+            // two threads per path (separate copies of the loop): every thread
+            // arrives on ABAR; warp 0 waits as a whole, so lane 0 never waits
+            // behind lanes of its own warp suspended on DBAR
+            o.l("sde_mbar_arrive(ABAR);");
+            if (half == 0) {
+                o.l("if (threadIdx.x < 32) {");
+                o.l("  const bool a_ready = sde_mbar_wait_bounded(ABAR, tc_phase);");
+                o.l("  if (!a_ready) tc_ok = 0;");
+                o.l("  if (threadIdx.x == 0 && a_ready) {");
+                o.l("    sde_tc_fence_after();");
+                issue("    ");
+                o.l("  }");
+                o.l("}");
+            }
         }
+        // lanes 1..31 of warp 0 must not suspend on DBAR before lane 0 has
+        // issued
+        if (half == 0) o.l("__syncwarp();");
         // while the MMA runs: the next group's Sobol high parts
         if (xorm() && g == group() - 1) hv_prefetch(o, "chunk0 + " + S((group() * NI) / 32));
         o.l("if (!sde_mbar_wait_bounded(DBAR, tc_phase)) tc_ok = 0;");
         o.l("tc_phase ^= 1u;");
-        // a warp leaves together (tcgen05.ld below is warp-collective)
-        o.l("if (!__all_sync(0xffffffffu, tc_ok)) break;");
+        if (mma->split == 1)  // a timed-out thread carries on; the next vote ends the loop for all
+            o.l("__syncwarp();");
+        else  // a warp leaves together (tcgen05.ld below is warp-collective)
+            o.l("if (!__all_sync(0xffffffffu, tc_ok)) break;");
         o.l("sde_tc_fence_after();");
         o.l("float DM[" + S(PH) + "];");
         // 16 columns per load: a block of D is consumed before the next one
@@ -759,8 +777,10 @@ struct Gen {
         o.l("unsigned char* const SBL = SBH + " + S(NP * KP * 2) + ";");
         o.l("sde_u64* const MBP = (sde_u64*)(SBL + " + S(NP * KP * 2) + ");");
         o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 2);");
-        // ABAR: A written (every thread arrives); DBAR: product committed
+        // ABAR: A written (two threads per path: every thread arrives);
+        // DBAR: the step's product committed (one arrival, tcgen05.commit)
         o.l("const sde_u32 ABAR = sde_smem_addr(MBP), DBAR = sde_smem_addr(MBP + 1);");
+        o.l("(void)ABAR;");
         o.l("for (int e = threadIdx.x; e < " + S(2 * 128 * KP * 2 / 16) + "; e += " + S(TH) +
             ") ((uint4*)SAH)[e] = make_uint4(0u, 0u, 0u, 0u);");
         o.l("for (int e = threadIdx.x; e < " + S(2 * NP * KP * 2 / 16) + "; e += " + S(TH) +
@@ -820,8 +840,8 @@ struct Gen {
             plo = 0;
             phi = -1;
         }
-        // teardown: every thread arrives here; the loops above hold no
-        // CTA-wide barrier
+        // teardown: every thread arrives here (one thread per path: after the
+        // same votes; two: the loops hold no CTA barrier)
         o.l("sde_tc_fence_before();");
         o.l("const int tc_all = __syncthreads_and(tc_ok);");
         o.l("sde_tc_fence_after();");
@@ -946,14 +966,24 @@ struct Gen {
                 V("H") + ", lane);");
     }
 
+    // forward kernels on XOR-scrambled Sobol fetch each group's high parts
+    // one group ahead, so the direction-number loads are never waited for
+    // (CUDA-core kernels only where a group spans several steps: with one
+    // step per group the fetch lands no earlier and costs registers)
+    bool hv_pf() const { return xorm() && mode == Mode::Forward && (mma || group() >= 2); }
+
     void time_loop(Out& o) {
         const int U = group();
         const int nblocks = uses_chacha() ? (U * NI) / 8 : (xorm() ? (U * NI) / 32 : 0);
-        if (mma && xorm()) {
-            const std::vector<bool> need = own_chunks();
-            for (int c = 0; c < nblocks; ++c)
-                if (need[c]) o.l("sde_u32 " + V("hvn", c) + " = 0u;");
-            hv_prefetch(o, "0");
+        const std::vector<bool> need = hv_pf() ? own_chunks() : std::vector<bool>();
+        if (hv_pf()) {
+            for (int j = 0; j < ppt; ++j) {
+                lane(j);
+                for (int c = 0; c < nblocks; ++c)
+                    if (need[c]) o.l("sde_u32 " + V("hvn", c) + " = 0u;");
+                hv_prefetch(o, "0");
+            }
+            lane(0);
         }
         o.l("for (int t0 = 0; t0 < n_steps; t0 += " + S(U) + ") {");
         o.ind++;
@@ -970,7 +1000,11 @@ struct Gen {
             for (int j = 0; j < ppt; ++j) {
                 lane(j);
                 o.l("const sde_u32* " + V("LOp") + " = a.sobol_lo + (sde_u64)t0 * " + S(NI * 32) + "u + " + V("L") + ";");
-                for (int c = 0; c < nblocks; ++c) o.l("sde_u32 " + V("hv", c) + ";");
+                for (int c = 0; c < nblocks; ++c)
+                    o.l("sde_u32 " + V("hv", c) + (hv_pf() && need[c] ? " = " + V("hvn", c) : "") + ";");
+                // the next group's, now; the tensor-core step issues its own
+                // while the product runs
+                if (hv_pf() && !mma) hv_prefetch(o, "chunk0 + " + S(nblocks));
             }
         }
         std::vector<std::vector<bool>> done(ppt, std::vector<bool>(std::max(1, nblocks), false));
