@@ -697,6 +697,7 @@ struct Gen {
         o.l("float DM[" + S(PH) + "];");
         // 16 columns per load: a block of D is consumed before the next one
         // is loaded, so D and the state need not be live in full at once
+        // (one 32-column load was measured: no faster, more spills)
         for (int c = 0; c < PH; c += 16) o.l("sde_tmem_ld16_wait(TROW + " + S(c) + "u, DM + " + S(c) + ");");
         o.l("const float sdz = sdt * 0x1p-12f;");
         for (int p : u.levy)
