@@ -80,7 +80,12 @@ typedef struct sde_options {
                                lockstep (1, 2 or 4), 0 = 1                 */
     int32_t icdf;           /* SDE_ICDF_*          default AS26            */
     int32_t tensor_cores;   /* SDE_TC_*            default OFF             */
-    int32_t reserved[4];
+    int32_t adjoint_recompute; /* adjoint plans: 1 = draw the increments
+                               again in the reverse sweep; 0 (default) =
+                               keep the forward pass's increments in device
+                               memory when they fit in a quarter of the
+                               free memory (else draw them again)          */
+    int32_t reserved[3];
 } sde_options;
 
 /* TC_ON: when the plan is FP32 Euler-Maruyama, forward, one path per

@@ -1131,6 +1131,13 @@ struct Gen {
         if (uses_chacha()) o.l("sde_u64 cblk = ~0ull; sde_u32 CB[16];");
         o.l(R + "* CK = (" + R + "*)a.ckpt;");
         o.l("const sde_u64 ckrow = (sde_u64)rep * a.n_ckpt;");
+        // the forward pass's increments, [rep][t][k][path], when the run
+        // holds a buffer for them: the reverse sweep then reads them instead
+        // of drawing them again
+        o.l(R + "* INC = (" + R + "*)a.inc;");
+        auto inc_at = [&](int k) {
+            return "INC[(((sde_u64)rep * n_steps + t) * " + S(NI) + "ull + " + S(k) + "ull) * a.n_paths + i]";
+        };
         // forward pass with checkpoints
         o.l("for (int t = 0; t < n_steps; ++t) {");
         o.ind++;
@@ -1142,6 +1149,11 @@ struct Gen {
         uniforms_ra(o);
         wiener(o);
         step_reference(o);
+        if (NI > 0) {
+            o.l("if (INC && active) {");
+            for (int k = 0; k < NI; ++k) o.l("  " + inc_at(k) + " = " + inc_store_name(k) + ";");
+            o.l("}");
+        }
         o.ind--;
         o.l("}");
         // payoffs and the terminal adjoint of payoff 0
@@ -1168,11 +1180,23 @@ struct Gen {
         o.l("const int s = t - s0;");
         for (int p = 0; p < P; ++p) o.l("LX[s * " + S(P) + " + " + S(p) + "] = X" + S(p) + ";");
         step_header(o);
-        uniforms_ra(o);
-        wiener(o);
-        // record the stochastic increments (jump counts need the cache = X)
+        // the step's increments: stored by the forward pass, or drawn again
+        // (jump counts need the cache = X)
         for (int p : u.levy) o.l("C" + S(p) + " = X" + S(p) + ";");
-        poisson(o, "C", "tc");
+        if (NI > 0) {
+            o.l(R + " IV[" + S(NI) + "];");
+            o.l("if (INC) {");
+            for (int k = 0; k < NI; ++k) o.l("  IV[" + S(k) + "] = active ? " + inc_at(k) + " : " + L(0.0) + ";");
+            o.l("} else {");
+            o.ind++;
+            uniforms_ra(o);
+            wiener(o);
+            poisson(o, "C", "tc");
+            for (int k = 0; k < NI; ++k) o.l("IV[" + S(k) + "] = " + inc_store_name(k) + ";");
+            o.ind--;
+            o.l("}");
+            for (int k = 0; k < NI; ++k) o.l("const " + R + " " + inc_store_name(k) + " = IV[" + S(k) + "];");
+        }
         for (int k = 0; k < NI; ++k) o.l("LI[s * " + S(NI) + " + " + S(k) + "] = " + inc_store_name(k) + ";");
         for (int p : u.levy) {
             o.l(R + " N" + S(p) + " = X" + S(p) + ";");

@@ -28,6 +28,8 @@ typedef struct sde_args {
     double* partials;         /* [rep][gridDim.x][K][4] estimator partial sums       */
     float* ckpt;              /* adjoint checkpoints [rep][n_ckpt][P][n_paths]       */
     double* grad_partials;    /* [rep][gridDim.x][G][2] adjoint gradient partials   */
+    void* inc;                /* adjoint: the forward pass's increments
+                                 [rep][T-1][n_inc][n_paths], or NULL (recompute)    */
     int* status;              /* device status word (0 = ok)                         */
     sde_u64 n_paths;          /* paths per replicate                                 */
     sde_u64 path_base;        /* scenario index of path 0 of replicate 0             */

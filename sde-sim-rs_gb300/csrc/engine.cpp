@@ -314,6 +314,7 @@ struct sde_plan {
     int output = SDE_OUT_FULL;
     bool auto_block = true;  // block size chosen per run from the path count
     int mma_smem = 0;        // dynamic shared memory of a tensor-core forward kernel
+    bool adjoint_recompute = false;  // adjoint: never keep the forward increments
     std::string source;
     std::string fwd_name, adj_name;
     std::shared_ptr<sde::Cubin> cubin;
@@ -332,7 +333,7 @@ struct sde_result {
     sde::DBuf out;                 // engine-owned filtration
     void* out_ptr = nullptr;       // filtration (engine- or caller-owned)
     sde::DBuf args_dev;            // staged time grid etc.
-    sde::DBuf partials, est_dev, masks, ckpt;
+    sde::DBuf partials, est_dev, masks, ckpt, inc;
     sde::HBuf est_host;
     sde::HBuf stage;               // pinned inputs, alive until the run is done
     cudaStream_t stream = nullptr;
@@ -405,6 +406,8 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
     p->spec = spec_from(&o);
     p->output = o.output;
     p->auto_block = o.block_size <= 0;
+    if (o.adjoint_recompute != 0 && o.adjoint_recompute != 1) fail(SDE_ERR_INVALID, "adjoint_recompute must be 0 or 1");
+    p->adjoint_recompute = o.adjoint_recompute == 1;
     for (const auto& s : payoffs) p->spec.payoffs.push_back(p->u.resolve(parse_expression(s)));
     if (grad_params || grad_x0) {
         if (p->spec.payoffs.empty()) fail(SDE_ERR_INVALID, "an adjoint plan needs a payoff");
@@ -621,6 +624,16 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         A.n_ckpt = std::max(1, (T - 1 + E - 1) / E);
         r->ckpt = DBuf((size_t)A.n_ckpt * std::max(1, P) * N * a.n_replicates * r->elem + 8);
         A.ckpt = r->ckpt.as<float>();
+        // the forward pass's increments [rep][T-1][NI][path], kept for the
+        // reverse sweep when they fit in a quarter of the free memory (the
+        // sweep otherwise draws them again: ChaCha blocks and normals)
+        const size_t inc_bytes = (size_t)(T - 1) * NI * N * a.n_replicates * r->elem;
+        size_t free_b = 0, total_b = 0;
+        if (!p->adjoint_recompute && inc_bytes > 0 && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+            inc_bytes <= free_b / 4) {
+            r->inc = DBuf(inc_bytes);
+            A.inc = r->inc.p;
+        }
     }
 
     const bool tc = tc_plan;

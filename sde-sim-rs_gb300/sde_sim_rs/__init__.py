@@ -156,11 +156,14 @@ class Plan:
                  scramble: str = "shift", precision: str = "fp64", semantics: str = "reference",
                  output: str = "full", block_size: int = 0, grad_params: Sequence[str] | None = None,
                  grad_x0: Sequence[str] | None = None, ckpt_every: int = 0, paths_per_thread: int = 1,
-                 icdf: str = "as26", tensor_cores: bool | str = False):
+                 icdf: str = "as26", tensor_cores: bool | str = False, adjoint_recompute: bool = False):
         """grad_params / grad_x0 make an adjoint plan: each run also returns
         the pathwise derivatives of E[payoffs[0]] with respect to those
         parameters and initial values (Euler-Maruyama, checkpoints every
-        ckpt_every steps, default 19).  tensor_cores=True lowers the dW
+        ckpt_every steps, default 19); the forward pass's increments are kept
+        in device memory for the reverse sweep when they fit in a quarter of
+        the free memory (adjoint_recompute=True draws them again instead).
+        tensor_cores=True lowers the dW
         terms of an FP32 Euler universe whose diffusions are constant * own
         process (correlated GBM) to one tcgen05 product per 128 paths, with
         two threads per path for wide universes ("row": always one);
@@ -177,6 +180,7 @@ class Plan:
         opts.output = N.OUTPUT[output]
         opts.block_size = block_size
         opts.ckpt_every = ckpt_every
+        opts.adjoint_recompute = 1 if adjoint_recompute else 0
         opts.paths_per_thread = paths_per_thread
         opts.icdf = N.ICDF[icdf]
         if tensor_cores not in N.TENSOR_CORES:

@@ -37,7 +37,7 @@ class Options(C.Structure):
                 ("scramble", C.c_int32), ("precision", C.c_int32), ("semantics", C.c_int32),
                 ("output", C.c_int32), ("block_size", C.c_int32), ("ckpt_every", C.c_int32),
                 ("paths_per_thread", C.c_int32), ("icdf", C.c_int32), ("tensor_cores", C.c_int32),
-                ("reserved", C.c_int32 * 4)]
+                ("adjoint_recompute", C.c_int32), ("reserved", C.c_int32 * 3)]
 
 
 class RunArgs(C.Structure):
