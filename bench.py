@@ -480,6 +480,25 @@ def run_basket(args):
     ps = n * 128
     nbytes = n * 64 * 32 * 4
     peak = _peaks()
+    # the compute fractions beside the HBM one: the lower-triangular K w is
+    # 2,080 FMA = 4,160 flop per path-step (the tensor pipe executes three
+    # split products of the full 64 x 64: 24,576 flop), against the measured
+    # bf16 tensor peak; 64 normals x 3 SFU ops (lg2, rsqrt, rcp) per
+    # path-step against the measured MUFU throughput
+    from sde_sim_rs import _native as N
+    import ctypes as C
+    sfu_peak = C.c_double()
+    N.check(N.lib().sde_probe_sfu_peak(C.byref(sfu_peak)))
+    flop_alg = 4160.0 * ps
+    sfu_ops = 192.0 * ps
+    compute = {
+        "tensor": {"achieved": flop_alg / (ms_step * 1e-3) / 1e12, "peak": peak.get("bf16_tflops"), "unit": "TFLOP/s",
+                   "frac": (flop_alg / (ms_step * 1e-3) / 1e12 / peak["bf16_tflops"]) if peak.get("bf16_tflops") else None,
+                   "algorithmic_flop_per_launch": flop_alg, "executed_flop_per_launch": 24576.0 * ps,
+                   "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"},
+        "sfu": {"achieved": sfu_ops / (ms_step * 1e-3) / 1e9, "peak": sfu_peak.value / 1e9, "unit": "Gop/s",
+                "frac": sfu_ops / (ms_step * 1e-3) / sfu_peak.value, "ops_per_launch": sfu_ops,
+                "peak_source": "measured by sde_probe_sfu_peak (MUFU throughput probe)"}}
     t0 = time.perf_counter()
     for _ in range(2):
         one().estimates()
@@ -501,6 +520,7 @@ def run_basket(args):
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
              "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, estimator only"},
             {"paths": n, "steps": 128, "checkpoints": 32, "price": price, "price_se": se,
+             "roofline_compute": compute,
              "kernel": "tcgen05 (3 x FP16 split, FP32 accumulate)" if main_leg["tc"] else "CUDA cores",
              "legs": {k: {"ms": v["ms"], "path_steps_per_s": ps / (v["ms"] * 1e-3), "price": v["price"],
                           "tensor_cores": v["tc"]} for k, v in legs.items()}})

@@ -219,6 +219,12 @@ int sde_result_copy_values(sde_result* r, double* host_out, int32_t layout);
  * NULL.  Built on the device, then copied.                                 */
 int sde_result_copy_long(sde_result* r, int32_t* scenario, double* time,
                          int32_t* process, double* value);
+/* The same rows in pinned host memory that the result owns: *n_rows rows
+ * per column, valid until sde_result_destroy.  Built on the device and
+ * copied once (later calls return the same arrays); a caller that wraps
+ * them (numpy, Arrow) copies nothing.                                     */
+int sde_result_long_host(sde_result* r, const int32_t** scenario, const double** time,
+                         const int32_t** process, const double** value, uint64_t* n_rows);
 /* Per replicate and estimator: sum and sum of squares of the payoff over
  * paths, FP64 with compensated summation; arrays
  * [n_replicates][sde_plan_n_estimates].                                   */

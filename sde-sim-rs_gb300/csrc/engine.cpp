@@ -336,6 +336,7 @@ struct sde_result {
     sde::DBuf partials, est_dev, masks, ckpt, inc;
     sde::HBuf est_host;
     sde::HBuf stage;               // pinned inputs, alive until the run is done
+    sde::HBuf long_host;           // pinned long-format columns (sde_result_long_host)
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     sde::DBuf status;              // kernel status word (tensor-core waits)
@@ -1009,6 +1010,44 @@ int sde_result_copy_long(sde_result* r, int32_t* scen, double* time, int32_t* pr
         if (value) cuda_check(cudaMemcpyAsync(value, dv.p, n * 8, cudaMemcpyDeviceToHost, r->stream), "D2H");
         cuda_check(cudaStreamSynchronize(r->stream), "D2H");
         r->waited = true;
+    });
+}
+
+int sde_result_long_host(sde_result* r, const int32_t** scen, const double** time, const int32_t** proc,
+                         const double** value, uint64_t* n_rows) {
+    return guarded([&] {
+        if (!r || !scen || !time || !proc || !value || !n_rows) fail(SDE_ERR_INVALID, "NULL argument");
+        const size_t n = (size_t)r->n_rep * r->n_paths * r->n_out * r->P;
+        *n_rows = n;
+        if (n == 0) {
+            *scen = nullptr; *time = nullptr; *proc = nullptr; *value = nullptr;
+            return;
+        }
+        if (!r->out_ptr) fail(SDE_ERR_INVALID, "the plan stores no filtration");
+        // one pinned block [scen i32][time f64][proc i32][value f64] per result
+        const size_t o_time = (n * 4 + 7) / 8 * 8, o_proc = o_time + n * 8, o_val = (o_proc + n * 4 + 7) / 8 * 8;
+        if (!r->long_host.p) {
+            r->long_host = HBuf(o_val + n * 8);
+            char* h = r->long_host.as<char>();
+            DBuf st(std::max<size_t>(1, r->slot_times.size()) * 8);
+            cuda_check(cudaMemcpyAsync(st.p, r->slot_times.data(), r->slot_times.size() * 8, cudaMemcpyHostToDevice,
+                                       r->stream),
+                       "slot times");
+            DBuf d(o_val + n * 8);
+            char* dd = d.as<char>();
+            cuda_check(launch_long_export(r->out_ptr, r->elem, r->n_paths, r->n_out, r->P, r->n_rep, st.as<double>(),
+                                          r->scen_base, (int32_t*)dd, (double*)(dd + o_time), (int32_t*)(dd + o_proc),
+                                          (double*)(dd + o_val), r->stream),
+                       "long export");
+            cuda_check(cudaMemcpyAsync(h, dd, o_val + n * 8, cudaMemcpyDeviceToHost, r->stream), "D2H");
+            cuda_check(cudaStreamSynchronize(r->stream), "D2H");
+            r->waited = true;
+        }
+        char* h = r->long_host.as<char>();
+        *scen = (const int32_t*)h;
+        *time = (const double*)(h + o_time);
+        *proc = (const int32_t*)(h + o_proc);
+        *value = (const double*)(h + o_val);
     });
 }
 

@@ -43,6 +43,16 @@ class Frame(dict):
         return self.height
 
 
+class _HostColumn:
+    """A column of engine-owned pinned memory as a numpy array interface;
+    numpy keeps this object (and with it the result owning the memory)
+    alive for as long as the array lives."""
+
+    def __init__(self, owner, ptr: int, n: int, typestr: str):
+        self._owner = owner
+        self.__array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, True), "version": 3}
+
+
 class Result:
     """One run: the filtration (on the device until copied) and estimators."""
 
@@ -91,16 +101,19 @@ class Result:
         return p.value, e.value
 
     def long(self) -> dict:
-        """Long columns in reference row order (scenario, time, process)."""
-        n = self.n_replicates * self.n_paths * self.n_out * self.n_processes
-        scen = np.zeros(n, dtype=np.int32)
-        time = np.zeros(n, dtype=np.float64)
-        proc = np.zeros(n, dtype=np.int32)
-        val = np.zeros(n, dtype=np.float64)
-        if n:
-            N.check(N.lib().sde_result_copy_long(self._h, scen.ctypes.data, time.ctypes.data,
-                                                 proc.ctypes.data, val.ctypes.data))
-        return {"scenario": scen, "time": time, "process": proc, "value": val}
+        """Long columns in reference row order (scenario, time, process):
+        read-only views of pinned host memory that this result owns (the
+        arrays keep it alive), so nothing is copied on the host."""
+        ptrs = [C.c_void_p() for _ in range(4)]
+        n = C.c_uint64()
+        N.check(N.lib().sde_result_long_host(self._h, *[C.byref(p) for p in ptrs], C.byref(n)))
+        cols = {}
+        for name, p, typestr in zip(("scenario", "time", "process", "value"), ptrs, ("<i4", "<f8", "<i4", "<f8")):
+            if n.value == 0:
+                cols[name] = np.zeros(0, dtype=np.dtype(typestr))
+            else:
+                cols[name] = np.asarray(_HostColumn(self, p.value, n.value, typestr))
+        return cols
 
     def estimates(self):
         """(sum, sumsq) arrays [replicates, payoffs] of the payoff estimators."""

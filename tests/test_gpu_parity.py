@@ -205,6 +205,19 @@ def test_long_format_rows(engine, oracle):
     assert cols["process"].tolist() == [p for _ in range(7 * 5) for p in range(3)]
     ref = oracle.Universe(EXAMPLE_PY).simulate(times, {"X0": 0.5, "X1": 100.0}, 3, 10, seed=1)
     assert close64(cols["value"], ref.reshape(n))[1] == 0
+    # the columns view pinned memory the result owns: read-only, and they
+    # keep the result alive after the caller drops it
+    assert not cols["value"].flags.writeable
+    expect = cols["value"].copy()
+    del res
+    import gc
+    gc.collect()
+    for _ in range(3):  # recycle pool memory in between
+        plan.run(times, {"X0": 1.5, "X1": 50.0}, 7, seed=9).long()
+    assert np.array_equal(cols["value"], expect)
+    # an empty run gives empty columns
+    empty = plan.run(times, {"X0": 0.5, "X1": 100.0}, 0).long()
+    assert all(len(c) == 0 for c in empty.values())
 
 
 def test_drop_in_simulate_frame(engine, oracle):
