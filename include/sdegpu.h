@@ -85,8 +85,17 @@ typedef struct sde_options {
                                keep the forward pass's increments in device
                                memory when they fit in a quarter of the
                                free memory (else draw them again)          */
-    int32_t reserved[3];
+    int32_t chunked;        /* SDE_CHUNKED_*       default AUTO            */
+    int32_t reserved[2];
 } sde_options;
+
+/* FP64 forward plans on pseudo or shifted-Sobol streams with 1, 2, 4 or 8
+ * stochastic indices also carry a chunked kernel for runs with few paths
+ * (the reference's 10,000): a CTA of 8 warps owns 32 paths, draws a chunk
+ * of steps' increments with all 8 warps, then steps the paths through it
+ * with one.  Same arithmetic, same results bit for bit.  AUTO uses it when
+ * the one-thread-per-path kernel would give fewer than 4 warps per SM.     */
+enum { SDE_CHUNKED_AUTO = 0, SDE_CHUNKED_ON = 1, SDE_CHUNKED_OFF = 2 };
 
 /* TC_ON: when the plan is FP32 Euler-Maruyama, forward, one path per
  * thread, without algebraic processes, and every dW coefficient is a

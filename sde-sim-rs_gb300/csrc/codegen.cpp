@@ -1078,6 +1078,108 @@ struct Gen {
         return o.s.str();
     }
 
+    // Forward kernel for runs with few paths (the reference's 10,000): one
+    // thread per path leaves most of the GPU idle and each thread runs a
+    // long chain of FP64 inverse CDFs.  Here a CTA of 8 warps owns 32 paths
+    // and walks the steps in chunks of 8 step groups.  Phase A: warp w draws
+    // group w of the chunk for all 32 paths (its ChaCha blocks, the FP64
+    // inverse CDFs) into shared memory.  Phase B: warp 0 steps the 32 paths
+    // through the chunk with the same step code as the one-thread-per-path
+    // kernel, reading the increments back, and stores the filtration.  The
+    // arithmetic is unchanged, so the paths are the same bit for bit.
+    // (NI dividing 8: a step group is one ChaCha block, and the two chunk
+    // buffers take 32 KB of static shared memory)
+    static bool chunked_eligible(const Universe& u, const KernelSpec& s) {
+        const int NI = u.n_stochastic();
+        return s.precision == PREC_FP64 && !s.adjoint && s.ppt == 1 && !s.tensor_cores &&
+               (s.rng == RNG_PSEUDO || s.scramble == SCRAMBLE_SHIFT) && NI > 0 && 8 % NI == 0;
+    }
+    std::string forward_chunked(const std::string& name) {
+        mode = Mode::Forward;
+        lane(0);
+        const int U = group(), CH = 8 * U;
+        const int NPAY = (int)sp.payoffs.size();
+        Out o;
+        o.l("extern \"C\" __global__ void __launch_bounds__(256) " + name + "(const sde_args a) {");
+        o.ind++;
+        // increments and uniforms of one chunk: [step][index][path]
+        o.l("__shared__ double SW[" + S(CH * NI * 32) + "];");
+        o.l("__shared__ double SU[" + S(CH * NI * 32) + "];");
+        o.l("const int warp = threadIdx.x >> 5;");
+        row = "lane";
+        cta = "32";
+        shared_prologue(o);
+        lane_prologue(o);
+        o.l("if (warp == 0) {");
+        store(o, "0");
+        o.l("}");
+        o.l("for (int c0 = 0; c0 < n_steps; c0 += " + S(CH) + ") {");
+        o.ind++;
+        // phase A: this warp's step group
+        o.l("{ const int t0 = c0 + warp * " + S(U) + ";");
+        o.ind++;
+        o.l("const sde_u64 blk0 = ((sde_u64)t0 * " + S(NI) + "ull) / 8ull;");
+        const int nblocks = (U * NI) / 8;
+        for (int b = 0; b < nblocks; ++b) o.l("sde_u32 " + V("B", b) + "[16];");
+        std::vector<bool> done(std::max(1, nblocks), false);
+        for (int g = 0; g < U; ++g) {
+            o.l("{ const int t = t0 + " + S(g) + ";");
+            o.l("if (t < n_steps) {");
+            o.ind++;
+            step_header(o);
+            uniforms(o, g, done);
+            wiener(o);
+            for (int k = 0; k < NI; ++k) {
+                const std::string at = "((warp * " + S(U) + " + " + S(g) + ") * " + S(NI) + " + " + S(k) + ") * 32 + lane";
+                if (u.token_kind[k] == IncKind::Dw) o.l("SW[" + at + "] = " + V("w", k) + ";");
+                o.l("SU[" + at + "] = " + V("u", k) + ";");
+            }
+            o.ind--;
+            o.l("} }");
+        }
+        o.ind--;
+        o.l("}");
+        o.l("__syncthreads();");
+        // phase B: warp 0 steps its 32 paths through the chunk
+        o.l("if (warp == 0) {");
+        o.ind++;
+        o.l("const int cend = min(" + S(CH) + ", n_steps - c0);");
+        o.l("for (int s = 0; s < cend; ++s) {");
+        o.ind++;
+        o.l("const int t = c0 + s;");
+        step_header(o);
+        for (int k = 0; k < NI; ++k) {
+            const std::string at = "(s * " + S(NI) + " + " + S(k) + ") * 32 + lane";
+            if (u.token_kind[k] == IncKind::Dw) o.l("const double " + V("w", k) + " = SW[" + at + "];");
+            o.l("const double " + V("u", k) + " = SU[" + at + "];");
+            o.l("(void)" + V("u", k) + ";");
+        }
+        step(o);
+        store(o, "t + 1");
+        o.ind--;
+        o.l("}");
+        o.ind--;
+        o.l("}");
+        o.l("__syncthreads();");
+        o.ind--;
+        o.l("}");
+        if (NPAY > 0) {
+            o.l("double fs[" + S(NPAY) + "] = {}, fq[" + S(NPAY) + "] = {};");
+            o.l("if (warp == 0) {");
+            o.ind++;
+            payoffs(o, NPAY);
+            o.ind--;
+            o.l("}");
+            o.l("sde_block_reduce_store<" + S(NPAY) + ">(fs, fq, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " +
+                S(NPAY) + "u) * 4u);");
+        }
+        row = "threadIdx.x";
+        cta = "blockDim.x";
+        o.ind--;
+        o.l("}");
+        return o.s.str();
+    }
+
     // Device function of one template for the batched kernel.
     std::string batch_template(const std::string& name, int K) {
         mode = Mode::Batch;
@@ -1309,6 +1411,8 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
 
 std::string forward_kernel_name(const KernelSpec& s) { return "sde_step_" + tag(s) + (s.tensor_cores ? "_tc" : ""); }
 std::string adjoint_kernel_name(const KernelSpec& s) { return "sde_adjoint_" + tag(s); }
+std::string chunked_kernel_name(const KernelSpec& s) { return "sde_step_" + tag(s) + "_chunked"; }
+bool has_chunked_kernel(const Universe& u, const KernelSpec& s) { return Gen::chunked_eligible(u, s); }
 
 std::string generate_source(const Universe& u, const KernelSpec& s) {
     Gen g(u, s);
@@ -1323,6 +1427,10 @@ std::string generate_source(const Universe& u, const KernelSpec& s) {
         return src;
     }
     src += g.forward(forward_kernel_name(s));
+    if (Gen::chunked_eligible(u, s)) {
+        Gen gc(u, s);
+        src += "\n" + gc.forward_chunked(chunked_kernel_name(s));
+    }
     if (s.adjoint) {
         KernelSpec s1 = s;
         s1.ppt = 1;

@@ -53,6 +53,12 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s);
 std::string forward_kernel_name(const KernelSpec& s);
 std::string adjoint_kernel_name(const KernelSpec& s);
 
+// FP64 forward plans on pseudo / shifted-Sobol streams also get a chunked
+// kernel for runs with few paths: a CTA of 8 warps per 32 paths draws a
+// chunk of steps' increments in parallel, then warp 0 steps through it.
+bool has_chunked_kernel(const Universe& u, const KernelSpec& s);
+std::string chunked_kernel_name(const KernelSpec& s);
+
 // CUDA C source of the kernels for one universe (without the runtime
 // header, which the JIT prepends).
 std::string generate_source(const Universe& u, const KernelSpec& s);

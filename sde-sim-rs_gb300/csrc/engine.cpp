@@ -300,6 +300,7 @@ struct Loaded {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t fwd = nullptr;
     cudaKernel_t adj = nullptr;
+    cudaKernel_t chk = nullptr;  // chunked forward kernel for small runs
 };
 
 // ---------------------------------------------------------------------------
@@ -315,6 +316,8 @@ struct sde_plan {
     bool auto_block = true;  // block size chosen per run from the path count
     int mma_smem = 0;        // dynamic shared memory of a tensor-core forward kernel
     bool adjoint_recompute = false;  // adjoint: never keep the forward increments
+    int chunked = SDE_CHUNKED_AUTO;  // small runs: the chunked kernel (when built)
+    std::string chk_name;            // empty: the plan has no chunked kernel
     std::string source;
     std::string fwd_name, adj_name;
     std::shared_ptr<sde::Cubin> cubin;
@@ -362,6 +365,8 @@ static Loaded& ensure_loaded(sde_plan* p) {
                        "tensor-core kernel shared memory");
         if (p->spec.adjoint)
             cuda_check(cudaLibraryGetKernel(&L.adj, L.lib, p->adj_name.c_str()), "cudaLibraryGetKernel");
+        if (!p->chk_name.empty())
+            cuda_check(cudaLibraryGetKernel(&L.chk, L.lib, p->chk_name.c_str()), "cudaLibraryGetKernel");
     }
     return L;
 }
@@ -409,6 +414,9 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
     p->auto_block = o.block_size <= 0;
     if (o.adjoint_recompute != 0 && o.adjoint_recompute != 1) fail(SDE_ERR_INVALID, "adjoint_recompute must be 0 or 1");
     p->adjoint_recompute = o.adjoint_recompute == 1;
+    if (o.chunked != SDE_CHUNKED_AUTO && o.chunked != SDE_CHUNKED_ON && o.chunked != SDE_CHUNKED_OFF)
+        fail(SDE_ERR_INVALID, "unknown chunked");
+    p->chunked = o.chunked;
     for (const auto& s : payoffs) p->spec.payoffs.push_back(p->u.resolve(parse_expression(s)));
     if (grad_params || grad_x0) {
         if (p->spec.payoffs.empty()) fail(SDE_ERR_INVALID, "an adjoint plan needs a payoff");
@@ -443,6 +451,7 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
     }
     p->fwd_name = forward_kernel_name(p->spec);
     p->adj_name = adjoint_kernel_name(p->spec);
+    if (has_chunked_kernel(p->u, p->spec) && p->chunked != SDE_CHUNKED_OFF) p->chk_name = chunked_kernel_name(p->spec);
     p->source = generate_source(p->u, p->spec);
     p->cubin = compile_cubin(p->source, p->spec.precision == PREC_FP32);
     return p.release();
@@ -474,18 +483,23 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     // the adjoint kernel steps one path per thread
     const int ppt_eff = p->spec.adjoint ? 1 : p->spec.ppt;
     int block = p->spec.block;
+    int dev = 0, sms = 148;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t warps = (N + 32ull * ppt_eff - 1) / (32ull * ppt_eff) * (uint64_t)a.n_replicates;
     if (p->auto_block) {
         // few paths (the reference's 10,000): spread the warps over every SM
         // rather than filling a few with 8-warp blocks
-        int dev = 0, sms = 148;
-        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const uint64_t warps = (N + 32ull * ppt_eff - 1) / (32ull * ppt_eff) * (uint64_t)a.n_replicates;
         const uint64_t wpb = std::min<uint64_t>(8, std::max<uint64_t>(1, (warps + sms - 1) / std::max(1, sms)));
         block = (int)(32 * wpb);
     }
+    // the chunked kernel (8 warps per 32 paths) when one thread per path
+    // would give fewer than 4 warps per SM
+    const bool use_chk = !p->chk_name.empty() && !p->spec.adjoint &&
+                         (p->chunked == SDE_CHUNKED_ON || warps < 4ull * (uint64_t)std::max(1, sms));
+    if (use_chk) block = 256;
     // a tensor-core CTA steps 128 paths (one MMA tile) with 128 or 256 threads
     const bool tc_plan = p->spec.tensor_cores && !p->spec.adjoint;
-    const uint64_t per_block = tc_plan ? 128ull : (uint64_t)block * ppt_eff;
+    const uint64_t per_block = tc_plan ? 128ull : use_chk ? 32ull : (uint64_t)block * ppt_eff;
     const uint64_t gx = (N + per_block - 1) / per_block;
     if (gx > 0x7fffffffull) fail(SDE_ERR_INVALID, "too many paths for one launch");
 
@@ -648,7 +662,7 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
 
     if (N > 0 && T >= 1) {
         void* kargs[] = {&A};
-        cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : L.fwd),
+        cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : use_chk ? L.chk : L.fwd),
                                     dim3((unsigned)gx, (unsigned)a.n_replicates), dim3(block), kargs,
                                     tc ? (size_t)p->mma_smem : 0, r->stream),
                    "step kernel launch");

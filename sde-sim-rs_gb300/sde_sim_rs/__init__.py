@@ -169,7 +169,8 @@ class Plan:
                  scramble: str = "shift", precision: str = "fp64", semantics: str = "reference",
                  output: str = "full", block_size: int = 0, grad_params: Sequence[str] | None = None,
                  grad_x0: Sequence[str] | None = None, ckpt_every: int = 0, paths_per_thread: int = 1,
-                 icdf: str = "as26", tensor_cores: bool | str = False, adjoint_recompute: bool = False):
+                 icdf: str = "as26", tensor_cores: bool | str = False, adjoint_recompute: bool = False,
+                 chunked: str = "auto"):
         """grad_params / grad_x0 make an adjoint plan: each run also returns
         the pathwise derivatives of E[payoffs[0]] with respect to those
         parameters and initial values (Euler-Maruyama, checkpoints every
@@ -180,7 +181,9 @@ class Plan:
         terms of an FP32 Euler universe whose diffusions are constant * own
         process (correlated GBM) to one tcgen05 product per 128 paths, with
         two threads per path for wide universes ("row": always one);
-        ``uses_tensor_cores`` says whether the universe was eligible."""
+        ``uses_tensor_cores`` says whether the universe was eligible.
+        chunked ("auto" | "on" | "off") picks the FP64 kernel for runs with
+        few paths, where 8 warps per 32 paths draw the increments."""
         if scheme not in N.SCHEME:
             raise ValueError(f"unknown scheme '{scheme}'")
         opts = N.Options()
@@ -194,6 +197,9 @@ class Plan:
         opts.block_size = block_size
         opts.ckpt_every = ckpt_every
         opts.adjoint_recompute = 1 if adjoint_recompute else 0
+        if chunked not in N.CHUNKED:
+            raise ValueError(f"unknown chunked {chunked!r}")
+        opts.chunked = N.CHUNKED[chunked]
         opts.paths_per_thread = paths_per_thread
         opts.icdf = N.ICDF[icdf]
         if tensor_cores not in N.TENSOR_CORES:

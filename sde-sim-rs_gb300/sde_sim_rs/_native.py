@@ -29,6 +29,7 @@ SEMANTICS = {"reference": 0, "textbook": 1}
 OUTPUT = {"full": 0, "checkpoints": 1, "terminal": 2, "none": 3}
 ICDF = {"as26": 0, "reference": 0, "accurate": 1}
 TENSOR_CORES = {False: 0, True: 1, "off": 0, "auto": 1, "row": 2}
+CHUNKED = {"auto": 0, "on": 1, "off": 2}
 LAYOUT_REFERENCE, LAYOUT_DEVICE = 0, 1
 
 
@@ -37,7 +38,7 @@ class Options(C.Structure):
                 ("scramble", C.c_int32), ("precision", C.c_int32), ("semantics", C.c_int32),
                 ("output", C.c_int32), ("block_size", C.c_int32), ("ckpt_every", C.c_int32),
                 ("paths_per_thread", C.c_int32), ("icdf", C.c_int32), ("tensor_cores", C.c_int32),
-                ("adjoint_recompute", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("adjoint_recompute", C.c_int32), ("chunked", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class RunArgs(C.Structure):
