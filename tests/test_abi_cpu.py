@@ -236,6 +236,31 @@ def test_tensor_core_lowering(engine, rng, scramble):
         assert "_tc(" not in r.source
 
 
+def test_chunked_kernel_lowering_and_options(engine):
+    """FP64 pseudo / shifted-Sobol plans with 1, 2, 4 or 8 stochastic indices
+    carry the chunked kernel for runs with few paths; others do not; option
+    values are checked."""
+    for eqs, rng, want in [(GBM, "pseudo", True), (HESTON, "sobol", True), (EXAMPLE_RS, "pseudo", True),
+                           (["dX = (0.1) * dW1 + (0.1) * dW2 + (0.1) * dW3"], "pseudo", False)]:
+        src = engine.Plan(eqs, rng=rng, precision="fp64").source
+        assert ("_chunked(const sde_args a)" in src) == want, (eqs, rng)
+    for kw in [dict(precision="fp32"), dict(rng="sobol", scramble="xor"), dict(paths_per_thread=2)]:
+        assert "_chunked(" not in engine.Plan(GBM, **kw).source, kw
+    src = engine.Plan(GBM, precision="fp64").source
+    assert "__shared__ double SW[2048]" in src        # 64 steps x 1 index x 32 paths
+    with pytest.raises(ValueError):
+        engine.Plan(GBM, chunked="sometimes")
+    from sde_sim_rs import _native as N
+    import ctypes as C
+    for field, bad in (("chunked", 7), ("adjoint_recompute", 2), ("tensor_cores", 5)):
+        opts = N.Options()
+        N.lib().sde_options_init(C.byref(opts))
+        setattr(opts, field, bad)
+        h = C.c_void_p()
+        rc = N.lib().sde_plan_create(N.cstrs(GBM), 1, N.cstrs([]), 0, N.cstrs([]), 0, C.byref(opts), C.byref(h))
+        assert rc == N.SDE_ERR_INVALID, field
+
+
 @pytest.mark.parametrize("ppt", [2, 4])
 def test_paths_per_thread_lowering(engine, ppt):
     from sde_sim_rs import _native as N
