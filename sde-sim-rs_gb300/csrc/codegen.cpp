@@ -606,9 +606,9 @@ struct Gen {
 
     bool linear_drift(int p, double& c) const { return linear_drift_of(u, p, c); }
 
-    // With two threads per path (mma->split == 2), the thread of half h
-    // draws the normals of A columns [h KP/2, (h+1) KP/2), reads D columns
-    // [h NP/2, (h+1) NP/2) and steps those processes.
+    // With S = mma->split threads per path (2 or 4), the thread of part h
+    // (`half`) draws the normals of A columns [h KP/S, (h+1) KP/S), reads D
+    // columns [h NP/S, (h+1) NP/S) and steps those processes.
     int half = 0;
     int kcols() const { return mma->kpad / mma->split; }
     int pcols() const { return mma->npad / mma->split; }
@@ -667,9 +667,9 @@ struct Gen {
             issue("  ");
             o.l("}");
         } else {
-            // two threads per path (separate copies of the loop): every thread
-            // arrives on ABAR; warp 0 waits as a whole, so lane 0 never waits
-            // behind lanes of its own warp suspended on DBAR
+            // several threads per path (separate copies of the loop): every
+            // thread arrives on ABAR; warp 0 waits as a whole, so lane 0 never
+            // waits behind lanes of its own warp suspended on DBAR
             o.l("sde_mbar_arrive(ABAR);");
             if (half == 0) {
                 o.l("if (threadIdx.x < 32) {");
@@ -778,7 +778,7 @@ struct Gen {
         o.l("unsigned char* const SBL = SBH + " + S(NP * KP * 2) + ";");
         o.l("sde_u64* const MBP = (sde_u64*)(SBL + " + S(NP * KP * 2) + ");");
         o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 2);");
-        // ABAR: A written (two threads per path: every thread arrives);
+        // ABAR: A written (several threads per path: every thread arrives);
         // DBAR: the step's product committed (one arrival, tcgen05.commit)
         o.l("const sde_u32 ABAR = sde_smem_addr(MBP), DBAR = sde_smem_addr(MBP + 1);");
         o.l("(void)ABAR;");
@@ -819,14 +819,15 @@ struct Gen {
             store(o, "0");
             time_loop(o);
         } else {
-            // each half steps its own processes in its own copy of the loop
-            // (its registers hold only those); the halves meet only at the
+            // each part steps its own processes in its own copy of the loop
+            // (its registers hold only those); the parts meet only at the
             // mbarriers, whose waits are bounded
-            for (int h = 0; h < 2; ++h) {
+            for (int h = 0; h < mma->split; ++h) {
                 half = h;
                 plo = h * pcols();
                 phi = std::min(P, (h + 1) * pcols());
-                o.l(h == 0 ? "if (half == 0) {" : "} else {");
+                o.l(h == 0 ? "if (half == 0) {"
+                           : h + 1 < mma->split ? "} else if (half == " + S(h) + ") {" : "} else {");
                 o.ind++;
                 lane_prologue(o);
                 store(o, "0");
@@ -842,7 +843,7 @@ struct Gen {
             phi = -1;
         }
         // teardown: every thread arrives here (one thread per path: after the
-        // same votes; two: the loops hold no CTA barrier)
+        // same votes; several: the loops hold no CTA barrier)
         o.l("sde_tc_fence_before();");
         o.l("const int tc_all = __syncthreads_and(tc_ok);");
         o.l("sde_tc_fence_after();");
@@ -886,7 +887,7 @@ struct Gen {
     }
 
     // Processes [plo, pend()) are this thread's (all but in the tensor-core
-    // kernel with two threads per path); `row` is the thread's path within
+    // kernel with several threads per path); `row` is the thread's path within
     // the CTA and `cta` the CTA's paths per lane.
     int plo = 0, phi = -1;
     int pend() const { return phi < 0 ? P : phi; }
@@ -1374,14 +1375,18 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
     std::vector<std::vector<double>> K;
     if (!diffusion_matrix(u, K)) return m;
     const int P = u.n_processes(), NI = u.n_stochastic();
-    // two threads per path for wide universes whose drifts are linear in
-    // their own process (each thread then needs only its half of the state)
+    // two or four threads per path for wide universes whose drifts are
+    // linear in their own process (each thread then needs only its part of
+    // the state)
     bool two = s.tensor_cores == 1 && P >= 32 && NI >= 32;
     for (int p = 0; two && p < P; ++p) {
         double c = 0.0;
         two = linear_drift_of(u, p, c);
     }
     for (int k = 0; two && k < NI; ++k) two = u.token_kind[k] == IncKind::Dw;
+    // (the kernel takes four too -- 512 threads, 64 registers, 32 warps per
+    // SM -- but on the 64-dim basket that measured 31.1 ms against 27.8 ms
+    // for two)
     m.split = two ? 2 : 1;
     const int nq = 16 * m.split;                            // each half's columns: multiples of 16
     m.npad = std::max(nq, (P + nq - 1) / nq * nq);          // M = 128 takes N = 16..256 in steps of 16
@@ -1390,7 +1395,7 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
     m.ncols = 32;
     while (m.ncols < m.npad) m.ncols *= 2;
     const int operands = 2 * 128 * m.kpad * 2 + 2 * m.npad * m.kpad * 2;
-    if (m.split == 2 && 128 * P * 4 > operands) {            // the payoff exchange reuses the operand area
+    if (m.split > 1 && 128 * P * 4 > operands) {             // the payoff exchange reuses the operand area
         m.split = 1;
         return mma_shape(u, [&] { KernelSpec t = s; t.tensor_cores = 2; return t; }());
     }
@@ -1402,9 +1407,10 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
     if (m.smem_bytes > 227 * 1024) return m;
     // CTAs per SM that the shared memory allows (1 KB reserved and 1 KB of
     // static reduction scratch each), capped by the register budget of
-    // __launch_bounds__: 128 registers a thread (one thread per path) or 85
-    // (two threads per path, 3 CTAs of 256)
-    m.min_blocks = std::max(1, std::min(m.split == 2 ? 3 : 4, 233472 / (m.smem_bytes + 2048)));
+    // __launch_bounds__: 128 registers a thread (one thread per path), 85
+    // (two, 3 CTAs of 256) or 64 (four, 2 CTAs of 512)
+    const int reg_cap = m.split == 1 ? 4 : m.split == 2 ? 3 : 2;
+    m.min_blocks = std::max(1, std::min(reg_cap, 233472 / (m.smem_bytes + 2048)));
     m.eligible = true;
     return m;
 }
