@@ -320,7 +320,11 @@ def run_engine(args):
             "fp64_gpu": fp64,
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
-                         "unit": "Gop/s", "frac": achieved / peak.value, "traffic": None,
+                         "unit": "Gop/s", "frac": achieved / peak.value,
+                         # ncu: ~160 KB DRAM read, 0 B written at 2^18 x 16 paths
+                         # (the quarter-size capture), x4 for a full launch
+                         "traffic": 4 * 160e3,
+                         "traffic_source": "profiles/sde_step_euler_fp32_sobolxor_heston_rqmc.md, scaled by paths",
                          "peak_source": "measured by sde_probe_sfu_peak (MUFU throughput probe)",
                          "algorithmic_ops_per_launch": sfu_ops},
             "cpu_baseline": {"value": cpu_v, "unit": "path-steps/s", "cores": os.cpu_count(),
@@ -440,7 +444,11 @@ def run_gbm_full(args):
              "d2h_bytes_per_step": rows * (4 + 8 + 4 + 8), "through": "sde_sim_rs.simulate (long frame)"},
             2 * args.steps,
             {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
-             "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"], "traffic": None,
+             "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],
+             # ncu of the chunked kernel at this size: 105 KB read; the 20 MB of
+             # filtration writes are still in L2 when the kernel ends
+             "traffic": 105216.0 if args.chunked != "off" else 106496.0,
+             "traffic_source": "profiles/sde_step_euler_fp64_pseudo_gbm_c0.md (full-size capture)",
              "note": "not a bandwidth case: the chunked kernel is bound by the FP64 pipe (80% busy in ncu; "
                      "~150 FP64 lane-ops per path-step, the FP64 inverse CDF), one thread per path by latency"},
             {"value": ps / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
@@ -524,7 +532,11 @@ def run_basket(args):
              "d2h_bytes_per_step": 16, "note": "filtration stays in HBM; the estimate is read back"},
             3 * args.steps,
             {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
-             "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"], "traffic": None,
+             "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],
+             # ncu of the tensor-core kernel at 2^17 paths: 1.012 GB written +
+             # 4.5 MB read, x16 for 2^21 paths (traffic grows with the paths)
+             "traffic": 16 * (1.012434e9 + 4.492e6) if main_leg["tc"] else None,
+             "traffic_source": "profiles/sde_step_basket64_tc_fp16.md, scaled by paths",
              "bytes_written_per_launch": nbytes},
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
              "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, estimator only"},
