@@ -47,6 +47,45 @@ def test_tensor_core_paths_match_cuda_core_kernel(engine, dim, layout, rng):
     assert np.allclose(sa, sb, rtol=2e-5) and np.allclose(qa, qb, rtol=4e-5)
 
 
+def _sparse_universe(P, NI, seed):
+    """P GBM-like processes driven by NI Wiener indices through random sparse
+    constant loadings (each process sees 3..8 of the indices, each index is
+    used): dS_i = (mu_i S_i) dt + sum_j (c_ij S_i) dW_j."""
+    rng = np.random.default_rng(seed)
+    eqs = []
+    used = set()
+    for i in range(P):
+        js = sorted(rng.choice(NI, size=int(rng.integers(3, 9)), replace=False).tolist())
+        if i == P - 1:  # every index appears somewhere (the registry numbers them in order of appearance)
+            js = sorted(set(js) | (set(range(NI)) - used))
+        used |= set(js)
+        terms = [f"({float(rng.uniform(0.0, 0.05))!r} * S{i + 1}) * dt"]
+        terms += [f"({float(rng.uniform(-0.2, 0.2))!r} * S{i + 1}) * dW{j + 1}" for j in js]
+        eqs.append(f"dS{i + 1} = " + " + ".join(terms))
+    return eqs
+
+
+@pytest.mark.parametrize("P,NI", [(32, 48), (48, 32), (33, 40)])
+@pytest.mark.parametrize("rng", ["pseudo", "sobol_xor"])
+def test_tensor_core_non_square_universes(engine, P, NI, rng):
+    """Processes and Wiener indices padded and split independently: more
+    indices than processes, fewer, and sizes just past a multiple of 32."""
+    eqs = _sparse_universe(P, NI, seed=P * 100 + NI)
+    r, s = RNGS[rng]
+    times = np.linspace(0.0, 1.0, 25)
+    init = {f"S{i + 1}": 50.0 + i for i in range(P)}
+    payoff = "max((" + " + ".join(f"S{i + 1}" for i in range(P)) + f") / {P} - 60, 0)"
+    tc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=r, scramble=s, tensor_cores=True)
+    cc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng=r, scramble=s)
+    assert tc.uses_tensor_cores and tc.n_stochastic == NI
+    a = tc.run(times, init, 700, seed=4).values()
+    b = cc.run(times, init, 700, seed=4).values()
+    assert np.max(np.abs(a - b) / np.abs(b)) < 2e-5
+    sa, _ = tc.run(times, init, 700, seed=4).estimates()
+    sb, _ = cc.run(times, init, 700, seed=4).estimates()
+    assert np.allclose(sa, sb, rtol=2e-5)
+
+
 @pytest.mark.parametrize("rng", ["pseudo", "sobol_xor"])
 def test_tensor_core_basket_against_fp64_oracle(engine, oracle, rng):
     dim = 8
