@@ -114,7 +114,11 @@ def dist_init(n_gpus):
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region.  The default timed region
+    of the Heston workload is under 100 ms, so the interval is short enough
+    to take several samples inside it."""
+
+    INTERVAL_MS = 25
 
     def __init__(self, gpu_index: int):
         self.path = tempfile.mktemp(suffix=".csv")
@@ -128,7 +132,7 @@ class Clocks:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -170,7 +174,7 @@ class Clocks:
                         reasons.add(n)
         os.unlink(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "interval_ms": self.INTERVAL_MS}
 
 
 def cpu_sample(threads: int, paths: int):

@@ -309,7 +309,17 @@ struct Gen {
                 tail53();
             }
         } else if (shiftm()) {
-            o.l("const sde_u32 " + V("x", k) + " = sde_sobol_direct(a.sobol_v, t * " + S(NI) + " + " + K + ", " + V("G") + ");");
+            // the dimension's point from the warp's two high parts (fetched
+            // once per 32 dimensions) and this lane's low part
+            o.l("const int " + V("sd", k) + " = t * " + S(NI) + " + " + K + ";");
+            o.l("if ((" + V("sd", k) + " >> 5) != " + V("shc") + ") { " + V("shc") + " = " + V("sd", k) + " >> 5; " +
+                V("shv0") + " = sde_sobol_hi_unrolled(a.sobol_vt, nullptr, a.sobol_dims, " + V("shc") + ", " +
+                V("sH0") + ", lane); " + V("shv1") + " = sde_sobol_hi_unrolled(a.sobol_vt, nullptr, a.sobol_dims, " +
+                V("shc") + ", " + V("sH1") + ", lane); }");
+            o.l("const sde_u32 " + V("sa", k) + " = __shfl_sync(0xffffffffu, " + V("shv0") + ", " + V("sd", k) + " & 31);");
+            o.l("const sde_u32 " + V("sb", k) + " = __shfl_sync(0xffffffffu, " + V("shv1") + ", " + V("sd", k) + " & 31);");
+            o.l("const sde_u32 " + V("x", k) + " = (" + V("shi1") + " ? " + V("sb", k) + " : " + V("sa", k) +
+                ") ^ __ldg(&a.sobol_lo[(sde_u64)" + V("sd", k) + " * 32u + " + V("sL") + "]);");
             if (!f32) {
                 o.l("const double " + V("v", k) + " = (double)" + V("x", k) + " * 0x1p-32 + sde_u64_to_f64(" + V("r", k) + ");");
                 o.l("const double " + V("u", k) + " = " + V("v", k) + " - trunc(" + V("v", k) + ");");
@@ -912,7 +922,23 @@ struct Gen {
         for (int p = plo; p < pend(); ++p) o.l(R + " " + V("C", p) + " = " + V("X", p) + ";");
         const std::string seed = mode == Mode::Forward ? "a.seed" : "in.seed";
         if (uses_chacha()) o.l("sde_u32 " + V("key") + "[8]; sde_seed_from_u64(" + seed + " + " + V("scen") + ", " + V("key") + ");");
-        if (shiftm()) o.l("const sde_u32 " + V("G") + " = sde_gray((sde_u32)(" + V("scen") + " + 5ull));");
+        if (shiftm()) {
+            // point n = scenario + 5 (the reference's skip(5)); gray(n) >> 5 ==
+            // gray(n >> 5), and a warp's 32 consecutive points fall in two
+            // groups of 32, W0 = lane 0's n >> 5 and W0 + 1.  The warp
+            // evaluates both groups' high parts for 32 dimensions at a time
+            // (sde_sobol_hi_unrolled); the low five bits of gray(n) index LO.
+            // Lanes past the last point may wrap n; they are inactive, and
+            // W0 + 1 beyond the table's 27 high bits reads nothing.
+            o.l("const sde_u32 " + V("sn") + " = (sde_u32)(" + V("scen") + " + 5ull);");
+            o.l("const sde_u32 " + V("sL") + " = sde_gray(" + V("sn") + ") & 31u;");
+            o.l("const sde_u32 " + V("sW0") + " = __shfl_sync(0xffffffffu, " + V("sn") + " >> 5, 0);");
+            o.l("const bool " + V("shi1") + " = (" + V("sn") + " >> 5) != " + V("sW0") + ";");
+            o.l("const sde_u32 " + V("sH0") + " = sde_gray(" + V("sW0") + ");");
+            o.l("const sde_u32 " + V("sH1") + " = " + V("sW0") + " + 1u < (1u << 27) ? sde_gray(" + V("sW0") +
+                " + 1u) : 0u;");
+            o.l("int " + V("shc") + " = -1; sde_u32 " + V("shv0") + " = 0u, " + V("shv1") + " = 0u;");
+        }
         if (xorm()) {
             o.l("const sde_u32 " + V("Gx") + " = sde_gray((sde_u32)" + V("i") + ");");
             o.l("const sde_u32 " + V("L") + " = " + V("Gx") + " & 31u, " + V("H") + " = " + V("Gx") + " >> 5;");

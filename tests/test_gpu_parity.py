@@ -237,6 +237,31 @@ def test_chunked_kernel_is_bit_identical(engine, eqs, init, scheme, rng):
     assert np.array_equal(a, b, equal_nan=True)
 
 
+@pytest.mark.parametrize("ppt,block", [(2, 0), (4, 0), (2, 64), (1, 512)])
+@pytest.mark.parametrize("precision,rng,scramble", [("fp64", "pseudo", "shift"), ("fp64", "sobol", "shift"),
+                                                    ("fp32", "sobol", "xor"), ("fp32", "pseudo", "shift")])
+def test_paths_per_thread_and_block_are_bit_identical(engine, ppt, block, precision, rng, scramble):
+    """Paths per thread and CTA size change only which thread steps a path:
+    the full filtration (1000 paths: a ragged last CTA and, with several
+    paths per thread, threads whose later paths are past the end) and the
+    estimator are those of one path per thread, bit for bit."""
+    times = np.linspace(0.0, 1.0, 41)
+    init = {"S": 100.0, "v": 0.04}
+    payoff = ["max(S - 100, 0)"]
+    kw = dict(rng=rng, scramble=scramble, precision=precision, payoffs=payoff)
+    base = engine.Plan(HESTON, **kw)
+    alt = engine.Plan(HESTON, paths_per_thread=ppt, block_size=block, **kw)
+    a = alt.run(times, init, 1000, seed=23, replicates=3)
+    b = base.run(times, init, 1000, seed=23, replicates=3)
+    assert np.array_equal(a.values(), b.values(), equal_nan=True)
+    ta = engine.Plan(HESTON, paths_per_thread=ppt, block_size=block, output="none", **kw)
+    tb = engine.Plan(HESTON, output="none", **kw)
+    sa, qa = ta.run(times, init, 5000, seed=23, replicates=3).estimates()
+    sb, qb = tb.run(times, init, 5000, seed=23, replicates=3).estimates()
+    # sums over the same path values; only the order of the FP64 additions differs
+    assert np.allclose(sa, sb, rtol=1e-12) and np.allclose(qa, qb, rtol=1e-12)
+
+
 def test_drop_in_simulate_frame(engine, oracle):
     times = [i / 252 for i in range(253)]
     fr = engine.simulate(GBM, times, 100, {"X": 100.0}, "pseudo", "euler", seed=42, output_format="numpy")
