@@ -77,7 +77,11 @@ typedef struct sde_options {
     int32_t ckpt_every;     /* adjoint plans: steps between checkpoints,
                                0 = 19                                      */
     int32_t paths_per_thread; /* independent paths a thread steps in
-                               lockstep (1, 2 or 4), 0 = 1                 */
+                               lockstep (1, 2 or 4); 0 = automatic: 1, or
+                               for FP32 XOR-Sobol plans without a set
+                               block_size, 2 in CTAs of 128 threads on runs
+                               of about 0.6M paths and more (same results
+                               bit for bit)                                */
     int32_t icdf;           /* SDE_ICDF_*          default AS26            */
     int32_t tensor_cores;   /* SDE_TC_*            default OFF             */
     int32_t adjoint_recompute; /* adjoint plans: 1 = draw the increments
@@ -238,6 +242,12 @@ int sde_result_long_host(sde_result* r, const int32_t** scenario, const double**
  * paths, FP64 with compensated summation; arrays
  * [n_replicates][sde_plan_n_estimates].                                   */
 int sde_result_estimates(sde_result* r, double* host_sum, double* host_sumsq);
+/* The step kernel the run launched: *kernel one of SDE_KERNEL_*, its CTA
+ * size and the paths one CTA steps (0 and 0 for a run without paths).  No
+ * counterpart in the reference.                                           */
+enum { SDE_KERNEL_NONE = 0, SDE_KERNEL_FORWARD = 1, SDE_KERNEL_CHUNKED = 2, SDE_KERNEL_WIDE = 3,
+       SDE_KERNEL_TENSOR_CORES = 4, SDE_KERNEL_ADJOINT = 5 };
+int sde_result_launch_info(const sde_result* r, int32_t* kernel, int32_t* block, int32_t* paths_per_block);
 
 /* ---- estimates with no device allocation --------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -1447,6 +1447,17 @@ std::string forward_kernel_name(const KernelSpec& s) { return "sde_step_" + tag(
 std::string adjoint_kernel_name(const KernelSpec& s) { return "sde_adjoint_" + tag(s); }
 std::string chunked_kernel_name(const KernelSpec& s) { return "sde_step_" + tag(s) + "_chunked"; }
 bool has_chunked_kernel(const Universe& u, const KernelSpec& s) { return Gen::chunked_eligible(u, s); }
+bool has_wide_kernel(const Universe& u, const KernelSpec& s) {
+    return s.wide && s.precision == PREC_FP32 && s.rng == RNG_SOBOL && s.scramble == SCRAMBLE_XOR && !s.adjoint &&
+           !s.tensor_cores && s.ppt == 1 && u.n_stochastic() > 0;
+}
+KernelSpec wide_spec(const KernelSpec& s) {
+    KernelSpec w = s;
+    w.ppt = 2;
+    w.block = 128;
+    w.wide = false;
+    return w;
+}
 
 std::string generate_source(const Universe& u, const KernelSpec& s) {
     Gen g(u, s);
@@ -1464,6 +1475,11 @@ std::string generate_source(const Universe& u, const KernelSpec& s) {
     if (Gen::chunked_eligible(u, s)) {
         Gen gc(u, s);
         src += "\n" + gc.forward_chunked(chunked_kernel_name(s));
+    }
+    if (has_wide_kernel(u, s)) {
+        const KernelSpec w = wide_spec(s);
+        Gen gw(u, w);
+        src += "\n" + gw.forward(forward_kernel_name(w));
     }
     if (s.adjoint) {
         KernelSpec s1 = s;

@@ -32,6 +32,8 @@ struct KernelSpec {
     std::vector<int> grad_params;       // parameter indices
     std::vector<int> grad_x0;           // process indices
     int ckpt_every = 19;                // steps between adjoint checkpoints
+    bool wide = false;                  // also build the two-paths-per-thread kernel
+                                        // (where has_wide_kernel allows it)
 };
 
 // Tensor-core lowering of correlated diffusions: eligible when the plan is
@@ -58,6 +60,12 @@ std::string adjoint_kernel_name(const KernelSpec& s);
 // chunk of steps' increments in parallel, then warp 0 steps through it.
 bool has_chunked_kernel(const Universe& u, const KernelSpec& s);
 std::string chunked_kernel_name(const KernelSpec& s);
+
+// FP32 forward plans on XOR-scrambled Sobol with spec.wide set also carry
+// a kernel that steps two paths per thread in CTAs of 128 threads, for runs
+// with many paths; wide_spec is its specification.
+bool has_wide_kernel(const Universe& u, const KernelSpec& s);
+KernelSpec wide_spec(const KernelSpec& s);
 
 // CUDA C source of the kernels for one universe (without the runtime
 // header, which the JIT prepends).

@@ -301,6 +301,7 @@ struct Loaded {
     cudaKernel_t fwd = nullptr;
     cudaKernel_t adj = nullptr;
     cudaKernel_t chk = nullptr;  // chunked forward kernel for small runs
+    cudaKernel_t wide = nullptr; // two paths per thread, for large runs
 };
 
 // ---------------------------------------------------------------------------
@@ -318,6 +319,7 @@ struct sde_plan {
     bool adjoint_recompute = false;  // adjoint: never keep the forward increments
     int chunked = SDE_CHUNKED_AUTO;  // small runs: the chunked kernel (when built)
     std::string chk_name;            // empty: the plan has no chunked kernel
+    std::string wide_name;           // empty: the plan has no two-paths-per-thread kernel
     std::string source;
     std::string fwd_name, adj_name;
     std::shared_ptr<sde::Cubin> cubin;
@@ -345,6 +347,7 @@ struct sde_result {
     sde::DBuf status;              // kernel status word (tensor-core waits)
     sde::HBuf status_host;
     bool waited = false;
+    int kernel = SDE_KERNEL_NONE, block = 0, per_block = 0;  // what the run launched
 };
 
 namespace sde {
@@ -367,6 +370,8 @@ static Loaded& ensure_loaded(sde_plan* p) {
             cuda_check(cudaLibraryGetKernel(&L.adj, L.lib, p->adj_name.c_str()), "cudaLibraryGetKernel");
         if (!p->chk_name.empty())
             cuda_check(cudaLibraryGetKernel(&L.chk, L.lib, p->chk_name.c_str()), "cudaLibraryGetKernel");
+        if (!p->wide_name.empty())
+            cuda_check(cudaLibraryGetKernel(&L.wide, L.lib, p->wide_name.c_str()), "cudaLibraryGetKernel");
     }
     return L;
 }
@@ -393,6 +398,8 @@ static KernelSpec spec_from(const sde_options* o) {
     if (s.block % 32 != 0 || s.block > 1024) fail(SDE_ERR_INVALID, "block_size must be a multiple of 32 up to 1024");
     s.ckpt_every = o->ckpt_every > 0 ? o->ckpt_every : 19;
     s.ppt = o->paths_per_thread > 0 ? o->paths_per_thread : 1;
+    // automatic: FP32 XOR-Sobol plans pick one or two paths per thread per run
+    s.wide = o->paths_per_thread == 0 && o->block_size <= 0;
     s.icdf = o->icdf;
     if (s.icdf != SDE_ICDF_AS26 && s.icdf != SDE_ICDF_ACCURATE) fail(SDE_ERR_INVALID, "unknown icdf");
     s.tensor_cores = o->tensor_cores;
@@ -452,6 +459,7 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
     p->fwd_name = forward_kernel_name(p->spec);
     p->adj_name = adjoint_kernel_name(p->spec);
     if (has_chunked_kernel(p->u, p->spec) && p->chunked != SDE_CHUNKED_OFF) p->chk_name = chunked_kernel_name(p->spec);
+    if (has_wide_kernel(p->u, p->spec)) p->wide_name = forward_kernel_name(wide_spec(p->spec));
     p->source = generate_source(p->u, p->spec);
     p->cubin = compile_cubin(p->source, p->spec.precision == PREC_FP32);
     return p.release();
@@ -499,7 +507,13 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     if (use_chk) block = 256;
     // a tensor-core CTA steps 128 paths (one MMA tile) with 128 or 256 threads
     const bool tc_plan = p->spec.tensor_cores && !p->spec.adjoint;
-    const uint64_t per_block = tc_plan ? 128ull : use_chk ? 32ull : (uint64_t)block * ppt_eff;
+    // two paths per thread in CTAs of 128 from 64 such warps per SM (about
+    // 0.6M paths on GB300): 3% faster on Heston at 2^20 x 4 and 2^18 x 16
+    // paths; runs of up to 2^18 paths are 10-15% faster with one
+    const bool use_wide = !p->wide_name.empty() && !use_chk && !tc_plan &&
+                          (N + 63) / 64 * (uint64_t)a.n_replicates >= 64ull * (uint64_t)std::max(1, sms);
+    if (use_wide) block = 128;
+    const uint64_t per_block = tc_plan ? 128ull : use_chk ? 32ull : use_wide ? 256ull : (uint64_t)block * ppt_eff;
     const uint64_t gx = (N + per_block - 1) / per_block;
     if (gx > 0x7fffffffull) fail(SDE_ERR_INVALID, "too many paths for one launch");
 
@@ -661,8 +675,12 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     }
 
     if (N > 0 && T >= 1) {
+        r->kernel = p->spec.adjoint ? SDE_KERNEL_ADJOINT : use_chk ? SDE_KERNEL_CHUNKED : use_wide ? SDE_KERNEL_WIDE
+                    : tc ? SDE_KERNEL_TENSOR_CORES : SDE_KERNEL_FORWARD;
+        r->block = block;
+        r->per_block = (int)per_block;
         void* kargs[] = {&A};
-        cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : use_chk ? L.chk : L.fwd),
+        cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : use_chk ? L.chk : use_wide ? L.wide : L.fwd),
                                     dim3((unsigned)gx, (unsigned)a.n_replicates), dim3(block), kargs,
                                     tc ? (size_t)p->mma_smem : 0, r->stream),
                    "step kernel launch");
@@ -1062,6 +1080,15 @@ int sde_result_long_host(sde_result* r, const int32_t** scen, const double** tim
         *time = (const double*)(h + o_time);
         *proc = (const int32_t*)(h + o_proc);
         *value = (const double*)(h + o_val);
+    });
+}
+
+int sde_result_launch_info(const sde_result* r, int32_t* kernel, int32_t* block, int32_t* per_block) {
+    return guarded([&] {
+        if (!r) fail(SDE_ERR_INVALID, "NULL result");
+        if (kernel) *kernel = r->kernel;
+        if (block) *block = r->block;
+        if (per_block) *per_block = r->per_block;
     });
 }
 

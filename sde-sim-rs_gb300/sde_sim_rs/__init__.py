@@ -115,6 +115,16 @@ class Result:
                 cols[name] = np.asarray(_HostColumn(self, p.value, n.value, typestr))
         return cols
 
+    KERNELS = {0: "none", 1: "forward", 2: "chunked", 3: "wide", 4: "tensor_cores", 5: "adjoint"}
+
+    def launch_info(self) -> dict:
+        """The step kernel this run launched ("forward", "chunked": 8 warps
+        per 32 paths, "wide": two paths per thread, "tensor_cores",
+        "adjoint"), its CTA size and the paths one CTA steps."""
+        k, b, pb = C.c_int32(), C.c_int32(), C.c_int32()
+        N.check(N.lib().sde_result_launch_info(self._h, C.byref(k), C.byref(b), C.byref(pb)))
+        return {"kernel": self.KERNELS[k.value], "block": b.value, "paths_per_block": pb.value}
+
     def estimates(self):
         """(sum, sumsq) arrays [replicates, payoffs] of the payoff estimators."""
         K = self._plan.n_payoffs if self._plan is not None else 0
@@ -168,7 +178,7 @@ class Plan:
                  payoffs: Sequence[str] = (), scheme: str = "euler", rng: str = "pseudo",
                  scramble: str = "shift", precision: str = "fp64", semantics: str = "reference",
                  output: str = "full", block_size: int = 0, grad_params: Sequence[str] | None = None,
-                 grad_x0: Sequence[str] | None = None, ckpt_every: int = 0, paths_per_thread: int = 1,
+                 grad_x0: Sequence[str] | None = None, ckpt_every: int = 0, paths_per_thread: int = 0,
                  icdf: str = "as26", tensor_cores: bool | str = False, adjoint_recompute: bool = False,
                  chunked: str = "auto"):
         """grad_params / grad_x0 make an adjoint plan: each run also returns
@@ -183,7 +193,9 @@ class Plan:
         two threads per path for wide universes ("row": always one);
         ``uses_tensor_cores`` says whether the universe was eligible.
         chunked ("auto" | "on" | "off") picks the FP64 kernel for runs with
-        few paths, where 8 warps per 32 paths draw the increments."""
+        few paths, where 8 warps per 32 paths draw the increments.
+        paths_per_thread 1, 2 or 4 fixes how many paths a thread steps; 0
+        (default) lets FP32 XOR-Sobol plans take two on large runs."""
         if scheme not in N.SCHEME:
             raise ValueError(f"unknown scheme '{scheme}'")
         opts = N.Options()

@@ -261,13 +261,33 @@ def test_chunked_kernel_lowering_and_options(engine):
         assert rc == N.SDE_ERR_INVALID, field
 
 
+def test_wide_kernel_lowering(engine):
+    """FP32 XOR-Sobol plans with automatic paths per thread (the default)
+    also carry a two-paths-per-thread kernel in CTAs of 128; a set
+    paths_per_thread or block_size, FP64, other streams, adjoint and
+    tensor-core plans do not."""
+    wide = "sde_step_euler_fp32_sobolxor_ppt2(const sde_args a)"
+    src = engine.Plan(HESTON, precision="fp32", rng="sobol", scramble="xor").source
+    assert wide in src and "sde_step_euler_fp32_sobolxor(const sde_args a)" in src
+    assert "__launch_bounds__(128) sde_step_euler_fp32_sobolxor_ppt2" in src
+    from bench import basket_equations
+    for eqs, kw in [(HESTON, dict(paths_per_thread=1)), (HESTON, dict(block_size=256)),
+                    (HESTON, dict(precision="fp64")), (HESTON, dict(scramble="shift")),
+                    (HESTON, dict(rng="pseudo", scramble="shift")),
+                    (GBM, dict(payoffs=["X"], grad_x0=["X"])),
+                    (basket_equations(8)[0], dict(tensor_cores=True))]:
+        args = dict(precision="fp32", rng="sobol", scramble="xor")
+        args.update(kw)
+        assert "_ppt2(" not in engine.Plan(eqs, **args).source, kw
+
+
 @pytest.mark.parametrize("ppt", [2, 4])
 def test_paths_per_thread_lowering(engine, ppt):
     from sde_sim_rs import _native as N
     import ctypes as C
     p = engine.Plan(["dv = (2 * (0.04 - max(v, 0))) * dt + (0.3 * max(v, 0)^0.5) * dW1",
                      "dS = (0.03 * S) * dt + (-0.7 * max(v, 0)^0.5 * S) * dW1"], payoffs=["S"],
-                    rng="sobol", scramble="xor", precision="fp32", output="terminal")
+                    rng="sobol", scramble="xor", precision="fp32", output="terminal", paths_per_thread=1)
     src = p.source
     assert "X1_1" not in src
     opts = N.Options()

@@ -262,6 +262,30 @@ def test_paths_per_thread_and_block_are_bit_identical(engine, ppt, block, precis
     assert np.allclose(sa, sb, rtol=1e-12) and np.allclose(qa, qb, rtol=1e-12)
 
 
+def test_automatic_wide_kernel(engine):
+    """FP32 XOR-Sobol plans with automatic paths per thread launch the
+    two-paths-per-thread kernel on large runs (here 2^16 paths x 16
+    replicates) and the one-path kernel on small ones; both give the
+    filtration of a plan fixed at one path per thread, bit for bit."""
+    times = np.linspace(0.0, 1.0, 9)
+    init = {"S": 100.0, "v": 0.04}
+    kw = dict(rng="sobol", scramble="xor", precision="fp32", payoffs=["max(S - 100, 0)"], output="terminal")
+    auto = engine.Plan(HESTON, **kw)
+    one = engine.Plan(HESTON, paths_per_thread=1, **kw)
+    for n, reps, kernel in [((1 << 16) - 3, 16, "wide"), (5000, 2, "forward")]:
+        a = auto.run(times, init, n, seed=9, replicates=reps)
+        b = one.run(times, init, n, seed=9, replicates=reps)
+        info = a.launch_info()
+        assert info["kernel"] == kernel, info
+        assert info["block"] == (128 if kernel == "wide" else info["block"])
+        assert info["paths_per_block"] == (256 if kernel == "wide" else info["block"])
+        assert b.launch_info()["kernel"] == "forward"
+        assert np.array_equal(a.values(), b.values())
+        sa, qa = a.estimates()
+        sb, qb = b.estimates()
+        assert np.allclose(sa, sb, rtol=1e-12) and np.allclose(qa, qb, rtol=1e-12)
+
+
 def test_drop_in_simulate_frame(engine, oracle):
     times = [i / 252 for i in range(253)]
     fr = engine.simulate(GBM, times, 100, {"X": 100.0}, "pseudo", "euler", seed=42, output_format="numpy")
