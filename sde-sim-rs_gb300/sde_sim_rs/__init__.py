@@ -154,10 +154,16 @@ class Result:
                     raise
         # rows cycle through the processes in order (src/filtration.rs:87-91),
         # so the name column is the name list tiled: fixed-width unicode, no
-        # per-row Python objects and no gather
+        # per-row Python objects and no gather.  One process: a read-only
+        # zero-stride view of the one name (like the other columns, which
+        # are read-only views of pinned memory), no copy at all
         ustr = np.asarray(list(self.process_names) or [""], dtype=str)
         P = max(1, self.n_processes)
-        names = np.tile(ustr[:P], len(cols["process"]) // P)
+        if P == 1:
+            names = np.broadcast_to(ustr[:1], (len(cols["process"]),))
+        else:
+            names = np.tile(ustr[:P], len(cols["process"]) // P)
+            names.flags.writeable = False
         return Frame(scenario=cols["scenario"], time=cols["time"], process_name=names, value=cols["value"])
 
 

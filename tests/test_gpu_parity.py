@@ -171,6 +171,32 @@ def test_replicates_and_offsets_are_scenario_ranges(engine, oracle):
     assert close64(b, ref[110:150])[1] == 0
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_shifted_sobol_offsets_and_high_indices(engine, oracle, precision):
+    """Shifted Sobol takes point s + 5 for scenario s, so a warp's 32 points
+    span two groups of 32 whose high parts the warp shares.  Path offsets
+    that are not multiples of 32, replicates that start inside a warp, and
+    point indices up to the 2^32 limit give the oracle's paths (FP64: bit
+    level; FP32 from the same uniforms: FP32 accuracy)."""
+    times = np.linspace(0, 1, 41)
+    init = {"S": 100.0, "v": 0.04}
+    plan = engine.Plan(HESTON, rng="sobol", precision=precision, chunked="off")
+    u = oracle.Universe(HESTON)
+    for offset, n, reps in [(77, 45, 3), (2**31 - 19, 64, 1), (2**32 - 5 - 200, 100, 2)]:
+        gpu = plan.run(times, init, n, replicates=reps, seed=13, path_offset=offset).values("reference")
+        ref = u.simulate(times, init, offset, offset + n * reps, rng=oracle.SOBOL, seed=13, threads=THREADS)
+        gpu = gpu.reshape(n * reps, len(times), 2)
+        if precision == "fp64":
+            assert close64(gpu, ref)[1] == 0, offset
+        else:
+            scale = np.maximum(np.abs(ref), np.abs(ref).mean(axis=0, keepdims=True))
+            rel = np.abs(gpu - ref) / scale
+            # the same bar as the other FP32 paths against the FP64 oracle
+            assert np.mean(rel < 1e-3) > 0.99, (offset, np.percentile(rel, [50, 99, 100]))
+    with pytest.raises(Exception, match="beyond 2"):
+        plan.run(times, init, 100, replicates=2, seed=13, path_offset=2**32 - 5 - 199)
+
+
 def test_xor_replicates_match_oracle(engine, oracle):
     times = np.linspace(0, 1, 65)
     plan = engine.Plan(HESTON, rng="sobol", scramble="xor")
@@ -302,6 +328,12 @@ def test_drop_in_simulate_frame(engine, oracle):
     ref3 = oracle.Universe(GBM).simulate(times, {"X": 100.0}, 0, 50, seed=42, rng=oracle.SOBOL,
                                          scheme=oracle.RK)
     assert close64(fr3["value"], ref3.reshape(-1))[1] == 0
+    # the name column: one name for one process (a read-only view), the
+    # names cycling in universe order for several
+    assert not fr["process_name"].flags.writeable and len(fr["process_name"]) == 100 * 253
+    fr4 = engine.simulate(HESTON, times[:5], 3, {"S": 100.0, "v": 0.04}, "pseudo", "euler", seed=1,
+                          output_format="numpy")
+    assert list(fr4["process_name"]) == ["v", "S"] * 15 and not fr4["process_name"].flags.writeable
 
 
 def test_estimators_fp64_match_oracle(engine, oracle):
