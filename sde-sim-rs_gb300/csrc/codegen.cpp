@@ -287,6 +287,9 @@ struct Gen {
         return u.token_kind[k] == IncKind::Dn || (sp.scheme == SCHEME_RK && k == 0) || sp.icdf != 0;
     }
     bool uses_chacha() const { return NI > 0 && !xorm(); }
+    // XOR mode: dimensions per LO load, the largest of 4, 2, 1 dividing NI
+    // (a step's first dimension is then aligned to it)
+    int lo_width() const { return NI % 4 == 0 ? 4 : NI % 2 == 0 ? 2 : 1; }
     bool has_alg() const { return !u.alg.empty(); }
 
     // ---- uniforms of step t for the current lane ------------------------
@@ -319,7 +322,8 @@ struct Gen {
             o.l("const sde_u32 " + V("sa", k) + " = __shfl_sync(0xffffffffu, " + V("shv0") + ", " + V("sd", k) + " & 31);");
             o.l("const sde_u32 " + V("sb", k) + " = __shfl_sync(0xffffffffu, " + V("shv1") + ", " + V("sd", k) + " & 31);");
             o.l("const sde_u32 " + V("x", k) + " = (" + V("shi1") + " ? " + V("sb", k) + " : " + V("sa", k) +
-                ") ^ __ldg(&a.sobol_lo[(sde_u64)" + V("sd", k) + " * 32u + " + V("sL") + "]);");
+                ") ^ __ldg(&a.sobol_lo[(sde_u64)(" + V("sd", k) + " >> 2) * 128u + " + V("sL") + " * 4u + (" +
+                V("sd", k) + " & 3)]);");
             if (!f32) {
                 o.l("const double " + V("v", k) + " = (double)" + V("x", k) + " * 0x1p-32 + sde_u64_to_f64(" + V("r", k) + ");");
                 o.l("const double " + V("u", k) + " = " + V("v", k) + " - trunc(" + V("v", k) + ");");
@@ -333,7 +337,8 @@ struct Gen {
                 " >> 5; " + V("hval") + " = sde_sobol_hi(a.sobol_vt, mask_rep, a.sobol_dims, " + V("hchunk") +
                 ", " + V("H") + ", lane); }");
             o.l("const sde_u32 " + V("y", k) + " = __shfl_sync(0xffffffffu, " + V("hval") + ", " + V("d", k) +
-                " & 31) ^ __ldg(&a.sobol_lo[(sde_u64)" + V("d", k) + " * 32u + " + V("L") + "]);");
+                " & 31) ^ __ldg(&a.sobol_lo[(sde_u64)(" + V("d", k) + " >> 2) * 128u + " + V("L") + " * 4u + (" +
+                V("d", k) + " & 3)]);");
             if (!f32) o.l("const double " + V("u", k) + " = ((double)" + V("y", k) + " + 0.5) * 0x1p-32;");
             else o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_xor(" + V("y", k) +
                      ", " + V("q", k) + ", " + V("up", k) + ", " + V("gt", k) + ");");
@@ -354,8 +359,24 @@ struct Gen {
                             ", " + V("H") + ", lane);");
                     block_done[c] = true;
                 }
+                // this lane's LO words come lw dimensions per load (16 or 8
+                // bytes); lw divides NI, so a load never spans two steps and
+                // every call draws whole loads (chunks of 8 in the
+                // tensor-core step)
+                const int lw = lo_width(), e0 = e - e % lw;
+                const std::string at = S((e0 / 4) * 128 + e0 % 4);
+                std::string word;
+                if (lw == 1) {
+                    word = "__ldg(" + V("LOp") + " + " + at + ")";
+                } else {
+                    if (e % lw == 0)
+                        o.l("const uint" + S(lw) + " " + V("LW", e) + " = __ldg((const uint" + S(lw) + "*)(" + V("LOp") +
+                            " + " + at + "));");
+                    static const char* const comp[4] = {"x", "y", "z", "w"};
+                    word = V("LW", e0) + "." + comp[e % lw];
+                }
                 o.l("const sde_u32 " + V("y", k) + " = __shfl_sync(0xffffffffu, " + V("hv", c) + ", " + S(l) +
-                    ") ^ __ldg(" + V("LOp") + " + " + S(e * 32) + ");");
+                    ") ^ " + word + ";");
                 if (!f32) o.l("const double " + V("u", k) + " = ((double)" + V("y", k) + " + 0.5) * 0x1p-32;");
                 else if (needs_tail(k))
                     o.l("float " + V("q", k) + "; bool " + V("up", k) + ", " + V("gt", k) + "; sde_tail_xor(" +
@@ -1027,7 +1048,9 @@ struct Gen {
             o.l("const int chunk0 = (t0 * " + S(NI) + ") >> 5;");
             for (int j = 0; j < ppt; ++j) {
                 lane(j);
-                o.l("const sde_u32* " + V("LOp") + " = a.sobol_lo + (sde_u64)t0 * " + S(NI * 32) + "u + " + V("L") + ";");
+                // the group starts at dimension t0*NI, a multiple of 32
+                o.l("const sde_u32* " + V("LOp") + " = a.sobol_lo + (sde_u64)t0 * " + S(NI * 32) + "u + " + V("L") +
+                    " * 4u;");
                 for (int c = 0; c < nblocks; ++c)
                     o.l("sde_u32 " + V("hv", c) + (hv_pf() && need[c] ? " = " + V("hvn", c) : "") + ";");
                 // the next group's, now; the tensor-core step issues its own

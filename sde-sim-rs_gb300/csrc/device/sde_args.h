@@ -22,7 +22,8 @@ typedef struct sde_args {
     const int* out_tidx;      /* [T]   output slot of time index t, or -1            */
     const sde_u32* sobol_v;   /* [dims][32] Joe-Kuo direction numbers                */
     const sde_u32* sobol_vt;  /* [32][dims] the same, transposed                     */
-    const sde_u32* sobol_lo;  /* [dims][32] xor of direction numbers 0..4 by 5 bits  */
+    const sde_u32* sobol_lo;  /* [dims/4][32][4]: xor of direction numbers 0..4 by
+                                 5 bits, four dimensions per low index      */
     const sde_u32* masks;     /* [n_rep][dims] XOR scramble masks                    */
     void* out;                /* [rep][n_out][P][n_paths] filtration slices          */
     double* partials;         /* [rep][gridDim.x][K][4] estimator partial sums       */

@@ -216,7 +216,11 @@ static SobolTables& sobol_tables(cudaStream_t stream) {
     auto& t = g_tables[dev];
     if (t) return *t;
     const int dims = kSobolMaxDims;
-    std::vector<uint32_t> V((size_t)dims * 32), VT((size_t)dims * 32), LO((size_t)dims * 32);
+    // LO: [dims/4][32 low indices][4 dimensions] -- a lane's words of four
+    // consecutive dimensions are one aligned 16-byte load, and a warp's 32
+    // lanes read 512 contiguous bytes; padded to a multiple of 4 dimensions
+    const int dims4 = (dims + 3) / 4 * 4;
+    std::vector<uint32_t> V((size_t)dims * 32), VT((size_t)dims * 32), LO((size_t)dims4 * 32, 0u);
     sobol_directions_host(dims, V.data());
     for (int d = 0; d < dims; ++d)
         for (int b = 0; b < 32; ++b) VT[(size_t)b * dims + d] = V[(size_t)d * 32 + b];
@@ -225,16 +229,16 @@ static SobolTables& sobol_tables(cudaStream_t stream) {
             uint32_t x = 0;
             for (int b = 0; b < 5; ++b)
                 if ((l >> b) & 1) x ^= V[(size_t)d * 32 + b];
-            LO[(size_t)d * 32 + l] = x;
+            LO[(size_t)(d >> 2) * 128 + (size_t)l * 4 + (d & 3)] = x;
         }
     auto nt = std::make_unique<SobolTables>();
     const size_t bytes = (size_t)dims * 32 * 4;
     nt->V = DBuf(bytes);
     nt->VT = DBuf(bytes);
-    nt->LO = DBuf(bytes);
+    nt->LO = DBuf((size_t)dims4 * 32 * 4);
     cuda_check(cudaMemcpyAsync(nt->V.p, V.data(), bytes, cudaMemcpyHostToDevice, stream), "upload Sobol V");
     cuda_check(cudaMemcpyAsync(nt->VT.p, VT.data(), bytes, cudaMemcpyHostToDevice, stream), "upload Sobol VT");
-    cuda_check(cudaMemcpyAsync(nt->LO.p, LO.data(), bytes, cudaMemcpyHostToDevice, stream), "upload Sobol LO");
+    cuda_check(cudaMemcpyAsync(nt->LO.p, LO.data(), LO.size() * 4, cudaMemcpyHostToDevice, stream), "upload Sobol LO");
     cuda_check(cudaStreamSynchronize(stream), "Sobol tables");
     nt->dims = dims;
     t = std::move(nt);
