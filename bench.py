@@ -325,9 +325,9 @@ def run_engine(args):
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
-                         # ncu: ~160 KB DRAM read, 0 B written at 2^18 x 16 paths
+                         # ncu: ~175 KB DRAM read, 0 B written at 2^18 x 16 paths
                          # (the quarter-size capture), x4 for a full launch
-                         "traffic": 4 * 160e3,
+                         "traffic": 4 * 174.6e3,
                          "traffic_source": "profiles/sde_step_euler_fp32_sobolxor_heston_rqmc.md, scaled by paths",
                          "peak_source": "measured by sde_probe_sfu_peak (MUFU throughput probe)",
                          "algorithmic_ops_per_launch": sfu_ops},
@@ -537,9 +537,9 @@ def run_basket(args):
             3 * args.steps,
             {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
              "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],
-             # ncu of the tensor-core kernel at 2^17 paths: 1.012 GB written +
-             # 4.5 MB read, x16 for 2^21 paths (traffic grows with the paths)
-             "traffic": 16 * (1.012434e9 + 4.492e6) if main_leg["tc"] else None,
+             # ncu of the tensor-core kernel at 2^17 paths: 1.014 GB written +
+             # 5.3 MB read, x16 for 2^21 paths (traffic grows with the paths)
+             "traffic": 16 * (1.013765e9 + 5.317e6) if main_leg["tc"] else None,
              "traffic_source": "profiles/sde_step_basket64_tc_fp16.md, scaled by paths",
              "bytes_written_per_launch": nbytes},
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
