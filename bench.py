@@ -325,10 +325,10 @@ def run_engine(args):
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
-                         # ncu: ~175 KB DRAM read, 0 B written at 2^18 x 16 paths
-                         # (the quarter-size capture), x4 for a full launch
-                         "traffic": 4 * 174.6e3,
-                         "traffic_source": "profiles/sde_step_euler_fp32_sobolxor_heston_rqmc.md, scaled by paths",
+                         # ncu (1 pass, full size): 183.8 KB DRAM read (the Sobol
+                         # tables and masks), 0 B written
+                         "traffic": 183.81e3,
+                         "traffic_source": "profiles/sde_step_euler_fp32_sobolxor_heston_rqmc.md (full-size capture)",
                          "peak_source": "measured by sde_probe_sfu_peak (MUFU throughput probe)",
                          "algorithmic_ops_per_launch": sfu_ops},
             "cpu_baseline": {"value": cpu_v, "unit": "path-steps/s", "cores": os.cpu_count(),
@@ -451,7 +451,7 @@ def run_gbm_full(args):
              "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],
              # ncu of the chunked kernel at this size: 105 KB read; the 20 MB of
              # filtration writes are still in L2 when the kernel ends
-             "traffic": 105216.0 if args.chunked != "off" else 106496.0,
+             "traffic": 104960.0 if args.chunked != "off" else 106496.0,
              "traffic_source": "profiles/sde_step_euler_fp64_pseudo_gbm_c0.md (full-size capture)",
              "note": "not a bandwidth case: the chunked kernel is bound by the FP64 pipe (80% busy in ncu; "
                      "~150 FP64 lane-ops per path-step, the FP64 inverse CDF), one thread per path by latency"},
@@ -537,10 +537,10 @@ def run_basket(args):
             3 * args.steps,
             {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
              "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],
-             # ncu of the tensor-core kernel at 2^17 paths: 1.014 GB written +
-             # 5.3 MB read, x16 for 2^21 paths (traffic grows with the paths)
-             "traffic": 16 * (1.013765e9 + 5.317e6) if main_leg["tc"] else None,
-             "traffic_source": "profiles/sde_step_basket64_tc_fp16.md, scaled by paths",
+             # ncu of the tensor-core kernel (1 pass, full size): 17.13 GB
+             # written + 68.9 MB read
+             "traffic": 17.13e9 + 68.86e6 if main_leg["tc"] else None,
+             "traffic_source": "profiles/sde_step_basket64_tc_fp16.md (full-size capture)",
              "bytes_written_per_launch": nbytes},
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
              "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, estimator only"},
