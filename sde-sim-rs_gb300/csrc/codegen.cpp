@@ -290,6 +290,21 @@ struct Gen {
     // XOR mode: dimensions per LO load, the largest of 4, 2, 1 dividing NI
     // (a step's first dimension is then aligned to it)
     int lo_width() const { return NI % 4 == 0 ? 4 : NI % 2 == 0 ? 2 : 1; }
+    // the tensor-core step reads its LO words from shared memory, where
+    // thread 0 bulk-copies each step's NI * 128 bytes two steps ahead
+    bool lo_tma() const { return mma && mma->lo_off > 0 && xorm() && mode == Mode::Forward; }
+    // thread 0: the bulk copy of step s's LO words into buffer s & 1
+    void lo_issue(Out& o, const std::string& pad, const std::string& s) const {
+        const std::string B = S(mma->lo_step_bytes) + "u";
+        o.l(pad + "if ((" + s + ") < a.T - 1) {");
+        o.l(pad + "  const sde_u32 b_ = (sde_u32)(" + s + ") & 1u;");
+        o.l(pad + "  sde_fence_async_smem();");
+        o.l(pad + "  sde_mbar_arrive_expect_tx(LBAR0 + 8u * b_, " + B + ");");
+        o.l(pad + "  sde_bulk_g2s(LOBA + b_ * " + B + ", a.sobol_lo + (sde_u64)(" + s + ") * " + S(NI * 32) + "ull, " + B +
+            ", LBAR0 + 8u * b_);");
+        o.l(pad + "  lb_issued = " + s + ";");
+        o.l(pad + "}");
+    }
     bool has_alg() const { return !u.alg.empty(); }
 
     // ---- uniforms of step t for the current lane ------------------------
@@ -366,7 +381,14 @@ struct Gen {
                 const int lw = lo_width(), e0 = e - e % lw;
                 const std::string at = S((e0 / 4) * 128 + e0 % 4);
                 std::string word;
-                if (lw == 1) {
+                if (lo_tma()) {
+                    // from the step's shared-memory buffer (k: the index in the step)
+                    const int k0q = k - k % 4;
+                    if (k % 4 == 0)
+                        o.l("const uint4 " + V("LW", k) + " = *(const uint4*)(" + V("LOS") + " + " + S(k0q / 4 * 512) + ");");
+                    static const char* const cq[4] = {"x", "y", "z", "w"};
+                    word = V("LW", k0q) + "." + cq[k % 4];
+                } else if (lw == 1) {
                     word = "__ldg(" + V("LOp") + " + " + at + ")";
                 } else {
                     if (e % lw == 0)
@@ -655,6 +677,13 @@ struct Gen {
 
     void step_mma(Out& o, int g, std::vector<bool>& done) const {
         const int KH = kcols(), PH = pcols();
+        if (lo_tma()) {
+            // this step's LO words, bulk-copied two steps ago
+            o.l("if (!sde_mbar_wait_bounded(LBAR0 + 8u * (sde_u32)(t & 1), (sde_u32)(t >> 1) & 1u)) tc_ok = 0;");
+            o.l("lb_waited = t;");
+            o.l("const unsigned char* const " + V("LOS") + " = LOB + (t & 1) * " + S(mma->lo_step_bytes) + " + " + V("L") +
+                " * 16u;");
+        }
         for (int k8 = half * KH; k8 < (half + 1) * KH; k8 += 8) {
             if (k8 < NI) {
                 uniforms(o, g, done, k8, std::min(k8 + 8, NI));
@@ -688,6 +717,9 @@ struct Gen {
                 o.l(pad + "sde_mma_f16(tmem, ADL + " + dc + ", BDH + " + dc + ", IDESC, 1u);");
             }
             o.l(pad + "sde_mma_commit(DBAR);");
+            // every thread has read this step's LO buffer (the A barrier):
+            // refill it with the words of step t + 2
+            if (lo_tma()) lo_issue(o, pad, "t + 2");
         };
         if (mma->split == 1) {
             // one thread per path: a CTA vote, the loop's only exit, so every
@@ -808,16 +840,31 @@ struct Gen {
         o.l("unsigned char* const SBH = SAL + " + S(128 * KP * 2) + ";");
         o.l("unsigned char* const SBL = SBH + " + S(NP * KP * 2) + ";");
         o.l("sde_u64* const MBP = (sde_u64*)(SBL + " + S(NP * KP * 2) + ");");
-        o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 2);");
+        o.l("sde_u32* const TSLOT = (sde_u32*)(MBP + 4);");
         // ABAR: A written (several threads per path: every thread arrives);
-        // DBAR: the step's product committed (one arrival, tcgen05.commit)
-        o.l("const sde_u32 ABAR = sde_smem_addr(MBP), DBAR = sde_smem_addr(MBP + 1);");
-        o.l("(void)ABAR;");
+        // DBAR: the step's product committed (one arrival, tcgen05.commit);
+        // LBAR0 / LBAR0 + 8: the two LO step buffers filled
+        o.l("const sde_u32 ABAR = sde_smem_addr(MBP), DBAR = sde_smem_addr(MBP + 1), LBAR0 = sde_smem_addr(MBP + 2);");
+        o.l("(void)ABAR; (void)LBAR0;");
+        o.l("int lb_issued = -1, lb_waited = -1;");
+        o.l("(void)lb_issued; (void)lb_waited;");
+        if (lo_tma()) {
+            o.l("const unsigned char* const LOB = sde_smem + " + S(mma->lo_off) + ";");
+            o.l("const sde_u32 LOBA = sde_smem_addr(LOB);");
+        }
         o.l("for (int e = threadIdx.x; e < " + S(2 * 128 * KP * 2 / 16) + "; e += " + S(TH) +
             ") ((uint4*)SAH)[e] = make_uint4(0u, 0u, 0u, 0u);");
         o.l("for (int e = threadIdx.x; e < " + S(2 * NP * KP * 2 / 16) + "; e += " + S(TH) +
             ") ((uint4*)SBH)[e] = ((const uint4*)" + name + "_kmat)[e];");
-        o.l("if (threadIdx.x == 0) { sde_mbar_init(ABAR, " + S(TH) + "u); sde_mbar_init(DBAR, 1u); sde_fence_mbar_init(); }");
+        o.l("if (threadIdx.x == 0) {");
+        o.l("  sde_mbar_init(ABAR, " + S(TH) + "u); sde_mbar_init(DBAR, 1u);");
+        if (lo_tma()) o.l("  sde_mbar_init(LBAR0, 1u); sde_mbar_init(LBAR0 + 8u, 1u);");
+        o.l("  sde_fence_mbar_init();");
+        if (lo_tma()) {
+            lo_issue(o, "  ", "0");
+            lo_issue(o, "  ", "1");
+        }
+        o.l("}");
         o.l("__syncwarp();");
         o.l("if (threadIdx.x < 32) sde_tmem_alloc(sde_smem_addr(TSLOT), " + S(mma->ncols) + "u);");
         o.l("sde_fence_async_smem();");
@@ -874,7 +921,11 @@ struct Gen {
             phi = -1;
         }
         // teardown: every thread arrives here (one thread per path: after the
-        // same votes; several: the loops hold no CTA barrier)
+        // same votes; several: the loops hold no CTA barrier).  A loop left
+        // early may leave LO copies in flight: thread 0 waits for them
+        if (lo_tma())
+            o.l("if (threadIdx.x == 0) for (int s_ = lb_waited + 1; s_ <= lb_issued; ++s_) "
+                "(void)sde_mbar_wait_bounded(LBAR0 + 8u * (sde_u32)(s_ & 1), (sde_u32)(s_ >> 1) & 1u);");
         o.l("sde_tc_fence_before();");
         o.l("const int tc_all = __syncthreads_and(tc_ok);");
         o.l("sde_tc_fence_after();");
@@ -1450,7 +1501,14 @@ MmaShape mma_shape(const Universe& u, const KernelSpec& s) {
         m.split = 1;
         return mma_shape(u, [&] { KernelSpec t = s; t.tensor_cores = 2; return t; }());
     }
-    const int need = operands + 32;                          // + two mbarriers and the TMEM address
+    int need = operands + 64;                                // + four mbarriers and the TMEM address
+    if (s.rng == RNG_SOBOL && s.scramble == SCRAMBLE_XOR && NI % 4 == 0) {
+        // the LO words of a step are NI * 128 contiguous bytes of the table:
+        // two step buffers, filled by bulk copies one step ahead
+        m.lo_off = (need + 127) / 128 * 128;
+        m.lo_step_bytes = NI * 128;
+        need = m.lo_off + 2 * m.lo_step_bytes;
+    }
     // at most 512 / ncols CTAs of an SM can hold tensor memory at once: ask
     // for enough shared memory (228 KB per SM) that no more are resident
     const int floor_bytes = 233472 / (512 / m.ncols + 1) + 1;

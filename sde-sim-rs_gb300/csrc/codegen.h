@@ -48,6 +48,9 @@ struct MmaShape {
     int smem_bytes = 0;   // dynamic shared memory of the kernel
     int min_blocks = 1;   // CTAs per SM the kernel is register-budgeted for
     int split = 1;        // threads per path (2: each steps half the processes)
+    int lo_off = 0;       // XOR Sobol, NI % 4 == 0: shared-memory offset of the two
+                          // step buffers of LO words (bulk-copied a step ahead); 0: none
+    int lo_step_bytes = 0;  // one step's LO words (NI * 128 bytes)
 };
 MmaShape mma_shape(const Universe& u, const KernelSpec& s);
 

@@ -385,6 +385,18 @@ SDE_DEV void sde_mbar_arrive(sde_u32 mbar) {
     asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(mbar) : "memory");
 }
 SDE_DEV void sde_fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+/* one arrival on a CTA mbarrier that also expects `bytes` of asynchronous
+ * copies to complete on it */
+SDE_DEV void sde_mbar_arrive_expect_tx(sde_u32 mbar, sde_u32 bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+/* bulk copy of `bytes` from global memory into this CTA's shared memory,
+ * completing on mbar; both addresses 16-byte aligned, bytes a multiple of 16 */
+SDE_DEV void sde_bulk_g2s(sde_u32 dst, const void* src, sde_u32 bytes, sde_u32 mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
 SDE_DEV void sde_tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 SDE_DEV void sde_tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
