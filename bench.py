@@ -537,9 +537,9 @@ def run_basket(args):
             3 * args.steps,
             {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
              "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],
-             # ncu of the tensor-core kernel (1 pass, full size): 17.13 GB
-             # written + 68.9 MB read
-             "traffic": 17.13e9 + 68.86e6 if main_leg["tc"] else None,
+             # ncu of the tensor-core kernel (1 pass, full size): 17.12 GB
+             # written + 38.2 MB read
+             "traffic": 17.12e9 + 38.16e6 if main_leg["tc"] else None,
              "traffic_source": "profiles/sde_step_basket64_tc_fp16.md (full-size capture)",
              "bytes_written_per_launch": nbytes},
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
