@@ -275,6 +275,25 @@ def run_engine(args):
         e2e_t.append(time.perf_counter() - t0)
     e2e_val = path_steps / statistics.median(e2e_t)
 
+    # the same workload on the reference's own Sobol mode (point s + 5 of
+    # scenario s, shifted by the scenario's ChaCha8 doubles), FP32 stepping
+    ps_plan = sde_sim_rs.Plan(HESTON, payoffs=[PAYOFF], rng="sobol", scramble="shift", precision="fp32",
+                              output="none")
+    one(ps_plan).estimates()
+    ms_sh = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.fill_(1)
+        e0.record(stream)
+        r_sh = one(ps_plan)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_sh.append(e0.elapsed_time(e1))
+    sh_price = float(r_sh.estimates()[0][:, 0].sum() / (npaths * reps))
+    shift_leg = {"value": path_steps / (statistics.median(ms_sh) * 1e-3), "unit": "path-steps/s",
+                 "ms": statistics.median(ms_sh), "estimate": sh_price,
+                 "note": "the reference's Sobol mode: point s+5, ChaCha8 shift per scenario and dimension"}
+
     # the plain FP64 GPU path on the same scrambled inputs (a sample of the
     # paths): its throughput and the FP32 estimate's deviation from it
     fp64 = None
@@ -322,6 +341,7 @@ def run_engine(args):
             "e2e": {"value": e2e_val, "unit": "path-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": reps * 16},
             "fp64_gpu": fp64,
+            "sobol_shift_fp32": shift_leg,
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
