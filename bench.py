@@ -465,7 +465,9 @@ def run_gbm_full(args):
     _common(args, "gbm_euler_fp64_10000x253_full", "path-steps/s (fwd, GBM full filtration, FP64)",
             ps / (ms_step * 1e-3), ms_step, "f64", clk.summary(),
             {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 253 * 28,
-             "d2h_bytes_per_step": rows * (4 + 8 + 4 + 8), "through": "sde_sim_rs.simulate (long frame)"},
+             "d2h_bytes_per_step": rows * 8, "through": "sde_sim_rs.simulate (long frame)",
+             "note": "the value column is copied every call; the scenario, time and process columns "
+                     "(16 B a row) are the shape's, copied once and shared by later calls of that shape"},
             2 * args.steps,
             {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
              "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],

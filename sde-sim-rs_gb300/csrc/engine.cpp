@@ -331,6 +331,20 @@ struct sde_plan {
     std::map<int, sde::Loaded> loaded;  // by device
 };
 
+namespace sde {
+// The scenario, time and process columns of long rows depend only on the
+// run's shape (replicates, paths, output slots and their times, processes,
+// first scenario), not on its values.  Results of the same shape share one
+// pinned copy of them, so a repeated drop-in call copies only its values.
+struct LongIndex {
+    uint64_t n_rep = 0, n_paths = 0, scen_base = 0;
+    int n_out = 0, P = 0;
+    std::vector<double> slot_times;
+    HBuf block;  // [scenario i32][time f64][process i32], 8-byte aligned columns
+    size_t o_time = 0, o_proc = 0, bytes = 0;
+};
+}  // namespace sde
+
 struct sde_result {
     std::shared_ptr<sde_plan> plan_keep;  // keeps the plan alive for one-shot runs
     sde_plan* plan = nullptr;
@@ -345,7 +359,8 @@ struct sde_result {
     sde::DBuf partials, est_dev, masks, ckpt, inc;
     sde::HBuf est_host;
     sde::HBuf stage;               // pinned inputs, alive until the run is done
-    sde::HBuf long_host;           // pinned long-format columns (sde_result_long_host)
+    sde::HBuf long_host;           // pinned long-format values (sde_result_long_host)
+    std::shared_ptr<const sde::LongIndex> long_index;  // the shape's pinned index columns
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     sde::DBuf status;              // kernel status word (tensor-core waits)
@@ -1049,6 +1064,65 @@ int sde_result_copy_long(sde_result* r, int32_t* scen, double* time, int32_t* pr
     });
 }
 
+namespace sde {
+static std::mutex g_lix_mu;
+static std::list<std::shared_ptr<LongIndex>> g_lix;  // most recent first
+static const size_t kLixMaxEntries = 8, kLixMaxBytes = (size_t)1 << 30;
+
+// The shape's index columns: from the cache, or exported on the result's
+// stream and copied into a new pinned block (then cached, least recently
+// used entries leaving beyond 8 shapes or 1 GiB; results keep theirs alive).
+static std::shared_ptr<const LongIndex> long_index(sde_result* r, size_t n) {
+    {
+        std::lock_guard<std::mutex> g(g_lix_mu);
+        for (auto it = g_lix.begin(); it != g_lix.end(); ++it) {
+            const LongIndex& e = **it;
+            if (e.n_rep == (uint64_t)r->n_rep && e.n_paths == r->n_paths && e.n_out == r->n_out && e.P == r->P &&
+                e.scen_base == r->scen_base && e.slot_times == r->slot_times) {
+                auto hit = *it;
+                g_lix.erase(it);
+                g_lix.push_front(hit);
+                return hit;
+            }
+        }
+    }
+    auto e = std::make_shared<LongIndex>();
+    e->n_rep = r->n_rep;
+    e->n_paths = r->n_paths;
+    e->scen_base = r->scen_base;
+    e->n_out = r->n_out;
+    e->P = r->P;
+    e->slot_times = r->slot_times;
+    e->o_time = (n * 4 + 7) / 8 * 8;
+    e->o_proc = e->o_time + n * 8;
+    e->bytes = e->o_proc + n * 4;
+    e->block = HBuf(e->bytes);
+    DBuf st(std::max<size_t>(1, r->slot_times.size()) * 8);
+    cuda_check(cudaMemcpyAsync(st.p, r->slot_times.data(), r->slot_times.size() * 8, cudaMemcpyHostToDevice, r->stream),
+               "slot times");
+    DBuf d(e->bytes);
+    char* dd = d.as<char>();
+    cuda_check(launch_long_export(r->out_ptr, r->elem, r->n_paths, r->n_out, r->P, r->n_rep, st.as<double>(),
+                                  r->scen_base, (int32_t*)dd, (double*)(dd + e->o_time), (int32_t*)(dd + e->o_proc),
+                                  nullptr, r->stream),
+               "long export (index columns)");
+    cuda_check(cudaMemcpyAsync(e->block.p, dd, e->bytes, cudaMemcpyDeviceToHost, r->stream), "D2H");
+    cuda_check(cudaStreamSynchronize(r->stream), "D2H");
+    std::lock_guard<std::mutex> g(g_lix_mu);
+    g_lix.push_front(e);
+    size_t total = 0, kept = 0;
+    for (auto it = g_lix.begin(); it != g_lix.end();) {
+        total += (*it)->bytes;
+        if (++kept > kLixMaxEntries || (kept > 1 && total > kLixMaxBytes)) {
+            it = g_lix.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    return e;
+}
+}  // namespace sde
+
 int sde_result_long_host(sde_result* r, const int32_t** scen, const double** time, const int32_t** proc,
                          const double** value, uint64_t* n_rows) {
     return guarded([&] {
@@ -1060,30 +1134,24 @@ int sde_result_long_host(sde_result* r, const int32_t** scen, const double** tim
             return;
         }
         if (!r->out_ptr) fail(SDE_ERR_INVALID, "the plan stores no filtration");
-        // one pinned block [scen i32][time f64][proc i32][value f64] per result
-        const size_t o_time = (n * 4 + 7) / 8 * 8, o_proc = o_time + n * 8, o_val = (o_proc + n * 4 + 7) / 8 * 8;
         if (!r->long_host.p) {
-            r->long_host = HBuf(o_val + n * 8);
-            char* h = r->long_host.as<char>();
-            DBuf st(std::max<size_t>(1, r->slot_times.size()) * 8);
-            cuda_check(cudaMemcpyAsync(st.p, r->slot_times.data(), r->slot_times.size() * 8, cudaMemcpyHostToDevice,
-                                       r->stream),
-                       "slot times");
-            DBuf d(o_val + n * 8);
-            char* dd = d.as<char>();
-            cuda_check(launch_long_export(r->out_ptr, r->elem, r->n_paths, r->n_out, r->P, r->n_rep, st.as<double>(),
-                                          r->scen_base, (int32_t*)dd, (double*)(dd + o_time), (int32_t*)(dd + o_proc),
-                                          (double*)(dd + o_val), r->stream),
+            // the values: exported on the device and copied once into a
+            // pinned block the result owns; the index columns are the shape's
+            r->long_index = long_index(r, n);
+            r->long_host = HBuf(n * 8);
+            DBuf dv(n * 8);
+            cuda_check(launch_long_export(r->out_ptr, r->elem, r->n_paths, r->n_out, r->P, r->n_rep, nullptr, 0,
+                                          nullptr, nullptr, nullptr, dv.as<double>(), r->stream),
                        "long export");
-            cuda_check(cudaMemcpyAsync(h, dd, o_val + n * 8, cudaMemcpyDeviceToHost, r->stream), "D2H");
+            cuda_check(cudaMemcpyAsync(r->long_host.p, dv.p, n * 8, cudaMemcpyDeviceToHost, r->stream), "D2H");
             cuda_check(cudaStreamSynchronize(r->stream), "D2H");
             r->waited = true;
         }
-        char* h = r->long_host.as<char>();
+        const char* h = r->long_index->block.as<char>();
         *scen = (const int32_t*)h;
-        *time = (const double*)(h + o_time);
-        *proc = (const int32_t*)(h + o_proc);
-        *value = (const double*)(h + o_val);
+        *time = (const double*)(h + r->long_index->o_time);
+        *proc = (const int32_t*)(h + r->long_index->o_proc);
+        *value = r->long_host.as<const double>();
     });
 }
 

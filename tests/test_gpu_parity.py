@@ -246,6 +246,35 @@ def test_long_format_rows(engine, oracle):
     assert all(len(c) == 0 for c in empty.values())
 
 
+def test_long_index_columns_are_shared_by_shape(engine):
+    """Results of one shape (replicates, paths, output times, processes,
+    first scenario) share one pinned copy of the scenario, time and process
+    columns; each has its own values.  Columns stay valid after the cache
+    has moved on past its 8 shapes, and a different first scenario or time
+    grid gets its own index."""
+    times = np.linspace(0, 1, 9)
+    plan = engine.Plan(HESTON)
+    init = {"S": 100.0, "v": 0.04}
+    a = plan.run(times, init, 50, seed=1).long()
+    b = plan.run(times, init, 50, seed=2).long()
+    for c in ("scenario", "time", "process"):
+        assert a[c].__array_interface__["data"][0] == b[c].__array_interface__["data"][0]
+    assert a["value"].__array_interface__["data"][0] != b["value"].__array_interface__["data"][0]
+    assert not np.array_equal(a["value"], b["value"])
+    shifted = plan.run(times, init, 50, seed=1, path_offset=7).long()
+    assert shifted["scenario"][0] == 7 and a["scenario"][0] == 0
+    regrid = plan.run(times * 2, init, 50, seed=1).long()
+    assert regrid["time"][-1] == 2.0 and a["time"][-1] == 1.0
+    keep = {c: a[c].copy() for c in a}
+    for k in range(12):  # more shapes than the cache holds
+        plan.run(times, init, 50 + k + 1, seed=3).long()
+    for c in a:
+        assert np.array_equal(a[c], keep[c])
+    again = plan.run(times, init, 50, seed=1).long()
+    for c in again:
+        assert np.array_equal(again[c], keep[c])
+
+
 @pytest.mark.parametrize("eqs,init", [(GBM, {"X": 100.0}), (HESTON, {"S": 100.0, "v": 0.04}),
                                       (EXAMPLE_RS, {"X1": 100.0}), (EXAMPLE_PY, {"X0": 0.5, "X1": 100.0})])
 @pytest.mark.parametrize("scheme", ["euler", "runge-kutta"])
