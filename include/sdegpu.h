@@ -232,10 +232,13 @@ int sde_result_copy_values(sde_result* r, double* host_out, int32_t layout);
  * NULL.  Built on the device, then copied.                                 */
 int sde_result_copy_long(sde_result* r, int32_t* scenario, double* time,
                          int32_t* process, double* value);
-/* The same rows in pinned host memory that the result owns: *n_rows rows
- * per column, valid until sde_result_destroy.  Built on the device and
- * copied once (later calls return the same arrays); a caller that wraps
- * them (numpy, Arrow) copies nothing.                                     */
+/* The same rows in pinned host memory: *n_rows rows per column, read-only,
+ * valid until sde_result_destroy.  Built on the device and copied once
+ * (later calls return the same arrays); a caller that wraps them (numpy,
+ * Arrow) copies nothing.  The values are the result's own; the scenario,
+ * time and process columns depend only on the run's shape and are shared
+ * by results of the same shape (the engine keeps the last 8 shapes, and a
+ * result keeps its own alive), so a repeated call copies only values.    */
 int sde_result_long_host(sde_result* r, const int32_t** scenario, const double** time,
                          const int32_t** process, const double** value, uint64_t* n_rows);
 /* Per replicate and estimator: sum and sum of squares of the payoff over
