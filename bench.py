@@ -475,8 +475,8 @@ def run_gbm_full(args):
              # filtration writes are still in L2 when the kernel ends
              "traffic": 104960.0 if args.chunked != "off" else 106496.0,
              "traffic_source": "profiles/sde_step_euler_fp64_pseudo_gbm_c0.md (full-size capture)",
-             "note": "not a bandwidth case: the chunked kernel is bound by the FP64 pipe (80% busy in ncu; "
-                     "~150 FP64 lane-ops per path-step, the FP64 inverse CDF), one thread per path by latency"},
+             "note": "not a bandwidth case: the chunked kernel is bound by the FP64 pipe (78% busy in ncu; "
+                     "~119 FP64 lane-ops per path-step, the FP64 inverse CDF), one thread per path by latency"},
             {"value": ps / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
              "sample": "full size (10,000 paths x 252 steps, full filtration)"},
             {"paths": n, "steps": 252, "chunked": args.chunked, "mean_XT": float(xt.mean()),
