@@ -471,9 +471,9 @@ def run_gbm_full(args):
             2 * args.steps,
             {"bound": "hbm", "achieved": nbytes / (ms_step * 1e-3) / 1e9, "peak": peak["hbm_gbs"], "unit": "GB/s",
              "frac": nbytes / (ms_step * 1e-3) / 1e9 / peak["hbm_gbs"],
-             # ncu of the chunked kernel at this size: 105 KB read; the 20 MB of
+             # ncu of the chunked kernel at this size: 151 KB read; the 20 MB of
              # filtration writes are still in L2 when the kernel ends
-             "traffic": 104960.0 if args.chunked != "off" else 106496.0,
+             "traffic": 150530.0 if args.chunked != "off" else 106496.0,
              "traffic_source": "profiles/sde_step_euler_fp64_pseudo_gbm_c0.md (full-size capture)",
              "note": "not a bandwidth case: the chunked kernel is bound by the FP64 pipe (78% busy in ncu; "
                      "~119 FP64 lane-ops per path-step, the FP64 inverse CDF), one thread per path by latency"},
