@@ -103,6 +103,26 @@ def test_stored_increments_match_recompute(engine, rng):
         assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
 
 
+@pytest.mark.parametrize("rng,scramble", [("sobol", "xor"), ("sobol", "shift"), ("pseudo", "shift")])
+def test_adjoint_forward_pass_uses_the_forward_kernels_inputs(engine, rng, scramble):
+    """The adjoint kernel draws a step's inputs by random access (a
+    segment's steps again in the recompute); its price, the forward pass's
+    payoff sum, is the forward kernel's on the same inputs to FP32
+    accuracy.  Different inputs (another Sobol point or scramble) would
+    move it by the Monte Carlo error, far more than this bar."""
+    params = {"kappa": 2.0, "theta": 0.04, "xi": 0.3, "rho": -0.7, "mu": 0.03}
+    init = {"S": 100.0, "v": 0.04}
+    times = np.linspace(0.0, 1.0, 101)
+    kw = dict(params=list(params), payoffs=["max(S - 100, 0)"], rng=rng, scramble=scramble, precision="fp32",
+              output="none")
+    adj = engine.Plan(HESTON_P, grad_params=["kappa", "xi"], grad_x0=["S"], ckpt_every=17, **kw)
+    fwd = engine.Plan(HESTON_P, **kw)
+    for n, reps in [(3000, 2), (1000, 3)]:
+        a = adj.run(times, init, n, replicates=reps, seed=21, params=params).estimates()[0][:, 0]
+        b = fwd.run(times, init, n, replicates=reps, seed=21, params=params).estimates()[0][:, 0]
+        assert np.allclose(a, b, rtol=2e-5), (a, b)
+
+
 def test_torch_autograd_function(engine):
     torch = pytest.importorskip("torch")
     from sde_sim_rs.adjoint import PathwisePricer
