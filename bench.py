@@ -419,6 +419,22 @@ def _timed_runs(fn, steps, stream, flush):
     return [a.elapsed_time(b) for a, b in ev], out
 
 
+def _chacha_roofline(path_steps_per_s, blocks_per_path_step, note, traffic):
+    """Roofline of a pseudo-random kernel: the ChaCha8 blocks it consumes per
+    second against the GPU's block rate measured by sde_probe_chacha8_rate
+    (the reference's generator is the bound: ALU / issue)."""
+    import ctypes as C
+    from sde_sim_rs import _native as N
+    peak = C.c_double()
+    N.check(N.lib().sde_probe_chacha8_rate(C.byref(peak)))
+    achieved = path_steps_per_s * blocks_per_path_step
+    return {"bound": "alu (ChaCha8)", "achieved": achieved / 1e9, "peak": peak.value / 1e9, "unit": "Gblock/s",
+            "frac": achieved / peak.value, "traffic": traffic,
+            "traffic_source": "profiles/sde_batch_and_adjoint_pseudo.md (full-size one-pass capture)",
+            "peak_source": "measured by sde_probe_chacha8_rate (every thread generates its own blocks)",
+            "algorithmic_blocks_per_path_step": blocks_per_path_step, "note": note}
+
+
 def _common(args, workload, metric, value, ms, dtype, clocks, e2e, launches, roofline, cpu, extra):
     line = {"metric": metric, "value": value, "unit": "path-steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -623,7 +639,13 @@ def run_batched(args):
             ps / (ms_step * 1e-3), ms_step, "f32", clk.summary(),
             {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
              "d2h_bytes_per_step": len(tid) * 16, "note": "graph replay + results read back"},
-            2 * args.steps, None, None,
+            2 * args.steps,
+            # one Wiener index per instance: one u64 per path-step, 1/8 block
+            _chacha_roofline(ps / (ms_step * 1e-3), 1.0 / 8.0,
+                             "each path-step draws one u64 of its scenario's ChaCha8 stream",
+                             # ncu (1 pass, the full 4096 instances): 3.48 MB read, 0 B written
+                             3.48e6),
+            None,
             {"instances": len(tid), "path_steps": ps, "block": job.block, "paths_per_thread": job.paths_per_thread,
              "work_items": job.n_items, "prepare_s": prep_s,
              "fp64_per_instance_launches": {"value": ps / fp64_s, "unit": "path-steps/s", "seconds": fp64_s},
@@ -654,8 +676,17 @@ def run_adjoint(args):
         for _ in range(args.warmup):
             one_a().wait()
         one_f().wait()
-        ms_a, ra = _timed_runs(one_a, args.steps, stream, flush)
+        with Clocks(0) as clk:
+            ms_a, ra = _timed_runs(one_a, args.steps, stream, flush)
         ms_f, rf = _timed_runs(one_f, 2, stream, flush)
+        # end to end through the public API: the run (pinned H2D of the time
+        # grid, parameters and initial values), the kernel, and the D2H of
+        # the price and gradient sums, host wall clock
+        e2e_t = []
+        for _ in range(max(3, args.steps // 2)):
+            t0 = time.perf_counter()
+            one_a().estimates()
+            e2e_t.append(time.perf_counter() - t0)
         s, q = ra[-1].estimates()
         m = s[0] / n
         se = np.sqrt(np.maximum(q[0] / n - m * m, 0) / n)
@@ -666,10 +697,25 @@ def run_adjoint(args):
                      "speedup_fp32_fwd_adj_vs_fp64_fwd": tf / ta,
                      "price_fp32": float(m[0]), "price_fp64": float(s64[0, 0] / n), "price_se": float(se[0]),
                      "gradients": dict(zip(gp + gx, [float(x) for x in m[1:]])),
-                     "gradient_se": dict(zip(gp + gx, [float(x) for x in se[1:]])), "ms": ta}
+                     "gradient_se": dict(zip(gp + gx, [float(x) for x in se[1:]])), "ms": ta,
+                     "e2e_path_steps_per_s": n * 365 / statistics.median(e2e_t), "clk": clk.summary(),
+                     "kt": 1 + len(gp) + len(gx)}
     g = out["gbm"]
+    clocks = g.pop("clk")
+    out["heston"].pop("clk")
+    h2d = (366 * 3 + 365 * 2) * 8 + 366 * (4 + 4) + 64
+    e2e = {"value": g["e2e_path_steps_per_s"], "unit": "path-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": g.pop("kt") * 16, "through": "Plan.run(...).estimates() (price and gradient sums)"}
+    out["heston"].pop("kt")
     _common(args, "adjoint_gbm_heston_2^20x365", "path-steps/s (fwd+adjoint, GBM, FP32)",
-            g["fwd_adjoint_path_steps_per_s"], g["ms"], "f32", None, None, 2 * args.steps, None, None, out)
+            g["fwd_adjoint_path_steps_per_s"], g["ms"], "f32", clocks, e2e, 2 * args.steps,
+            _chacha_roofline(g["fwd_adjoint_path_steps_per_s"], 1.0 / 8.0,
+                             "the forward pass draws one u64 per path-step; the reverse sweep reads the stored "
+                             "increments back and adds the recompute and adjoint arithmetic",
+                             # ncu (1 pass, GBM at 2^20 paths): 2.07 GB written (increments and
+                             # checkpoints) + 1.35 GB read (the rest of the increments hit L2)
+                             2.07e9 + 1.35e9),
+            None, out)
 
 
 def main():

@@ -327,6 +327,11 @@ int sde_sobol_directions(int32_t dims, uint32_t* host_out);
  * throughput in operations per second; the roofline denominator of the
  * terminal-only (SFU-bound) kernels.                                       */
 int sde_probe_sfu_peak(double* ops_per_second);
+/* Times a kernel in which every thread expands its own ChaCha8 key and
+ * generates consecutive 16-word blocks, and reports blocks per second; the
+ * roofline denominator of the pseudo-random kernels, whose bound is the
+ * reference's generator.                                                  */
+int sde_probe_chacha8_rate(double* blocks_per_second);
 
 #ifdef __cplusplus
 }

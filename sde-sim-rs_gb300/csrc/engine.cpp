@@ -1220,6 +1220,13 @@ int sde_probe_sfu_peak(double* ops) {
     });
 }
 
+int sde_probe_chacha8_rate(double* blocks) {
+    return guarded([&] {
+        if (!blocks) fail(SDE_ERR_INVALID, "NULL output");
+        cuda_check(run_chacha_probe(blocks), "ChaCha8 probe");
+    });
+}
+
 }  // extern "C"
 
 namespace sde {

@@ -242,6 +242,56 @@ __global__ void k_sfu_probe(float seed, float* __restrict__ sink) {
     if (r == 12345.678f) sink[threadIdx.x] = r;
 }
 
+// ChaCha8 block rate: each thread expands its own key (as a scenario does)
+// and generates ITER consecutive blocks, folding their words into one so
+// that none is dead; the roofline denominator of the pseudo-random kernels,
+// whose bound is the reference's generator.  (sink: 1024 words; only a
+// thread whose fold hits the magic value writes, at threadIdx.x < 256.)
+template <int ITER>
+__global__ void k_chacha_probe(sde_u64 seed, sde_u32* __restrict__ sink) {
+    sde_u32 key[8];
+    sde_seed_from_u64(seed + (sde_u64)blockIdx.x * blockDim.x + threadIdx.x, key);
+    sde_u32 acc = 0u;
+#pragma unroll 1
+    for (int i = 0; i < ITER; ++i) {
+        sde_u32 o[16];
+        sde_chacha8_block(key, (sde_u64)i, o);
+#pragma unroll
+        for (int w = 0; w < 16; ++w) acc ^= o[w];
+    }
+    if (acc == 0x9e3779b9u) sink[threadIdx.x] = acc;
+}
+
+cudaError_t run_chacha_probe(double* blocks_per_second) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    sde_u32* sink = nullptr;
+    e = cudaMalloc(&sink, 1024 * sizeof(sde_u32));
+    if (e != cudaSuccess) return e;
+    constexpr int ITER = 256;
+    const int threads = 256, blocks = sms * 8;
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    k_chacha_probe<ITER><<<blocks, threads>>>(1ull, sink);  // warm-up
+    cudaEventRecord(t0);
+    const int reps = 5;
+    for (int r = 0; r < reps; ++r) k_chacha_probe<ITER><<<blocks, threads>>>(7ull + (sde_u64)r * 1000003ull, sink);
+    cudaEventRecord(t1);
+    e = cudaEventSynchronize(t1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaFree(sink);
+    if (e != cudaSuccess) return e;
+    *blocks_per_second = (double)reps * blocks * threads * ITER / (ms * 1e-3);
+    return cudaGetLastError();
+}
+
 cudaError_t run_sfu_probe(double* ops_per_second) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);

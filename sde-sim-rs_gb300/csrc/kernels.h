@@ -36,5 +36,7 @@ cudaError_t launch_kat_icdf(const double* p, sde_u64 n, double* out, cudaStream_
 
 // SFU (MUFU) throughput probe: ops/s over a timed launch.
 cudaError_t run_sfu_probe(double* ops_per_second);
+// ChaCha8 block-rate probe: blocks/s over a timed launch.
+cudaError_t run_chacha_probe(double* blocks_per_second);
 
 }  // namespace sde

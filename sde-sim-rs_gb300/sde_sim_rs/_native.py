@@ -89,6 +89,7 @@ SIGNATURES = {
     "sde_plan_source": ([C.c_void_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
     "sde_plan_compile_log": ([C.c_void_p, C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
     "sde_plan_tensor_cores": ([C.c_void_p, C.POINTER(C.c_int32)], C.c_int),
+    "sde_probe_chacha8_rate": ([C.POINTER(C.c_double)], C.c_int),
     "sde_result_launch_info": ([C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
                                C.c_int),
     "sde_result_long_host": ([C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
