@@ -102,15 +102,17 @@ def build(verbose: bool = False) -> str:
         o = os.path.join(OBJ, src.replace(".cpp", ".o"))
         objs.append(o)
         s = os.path.join(HERE, src)
-        if _stale(o, [s] + headers):
+        if _stale(o, [s] + headers + [os.path.abspath(__file__)]):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
                          *inc, "-c", s, "-o", o])
     for src in ("kernels.cu", "noalloc.cu"):
         o = os.path.join(OBJ, src.replace(".cu", ".o"))
         objs.append(o)
         s = os.path.join(HERE, src)
-        if _stale(o, [s] + headers + [os.path.join(HERE, "engine_internal.h")]):
-            jobs.append(["nvcc", ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+        if _stale(o, [s] + headers + [os.path.join(HERE, "engine_internal.h"), os.path.abspath(__file__)]):
+            # -fmad=false: the known-answer kernels evaluate the FP64 inverse
+            # CDF exactly as the lowered FP64 kernels do (no contraction)
+            jobs.append(["nvcc", ARCH, "-O3", "-fmad=false", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                          *inc, "-c", s, "-o", o])
     procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
              for j in jobs]

@@ -65,9 +65,10 @@ def test_kat_icdf(engine, oracle):
     # near p = 0.5 the formula cancels (t - ratio, both ~1.18): a one-ulp
     # difference of log() is an absolute, not a relative, error there
     assert np.max(np.abs(out - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-14
-    # CUDA's FP64 log and glibc's differ by at most one ulp; most results
-    # are still bit-identical
-    assert np.mean(out == ref) > 0.5
+    # the device logarithm (table-driven, within 0.52 ulp) and the C
+    # library's differ by at most one ulp, and rarely: nearly every normal
+    # is bit-identical
+    assert np.mean(out == ref) > 0.98
 
 
 # ---------------------------------------------------------------- FP64 parity
@@ -476,3 +477,20 @@ def test_accurate_icdf_option(engine, oracle, rng):
                                         **_oracle_cfg(oracle, "euler", rng, "reference"))
     rel = np.abs(g32 - r32) / np.maximum(np.abs(r32), 1.0)
     assert np.mean(rel < 1e-3) > 0.99
+
+
+def test_roofline_probes(engine):
+    """The two roofline denominators the bench measures in its own run: the
+    SFU (MUFU) throughput and the ChaCha8 block rate, positive and within
+    what one GB300 can do (16 SFU ops and at most one 16-word block per
+    SM and clock)."""
+    import ctypes as C
+    from sde_sim_rs import _native as N
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    ops, blocks = C.c_double(), C.c_double()
+    N.check(N.lib().sde_probe_sfu_peak(C.byref(ops)))
+    N.check(N.lib().sde_probe_chacha8_rate(C.byref(blocks)))
+    clock = 2.2e9  # above the part's top SM clock
+    assert 0 < ops.value <= 16 * sms * clock
+    assert 0 < blocks.value <= sms * clock
