@@ -1109,10 +1109,20 @@ struct Gen {
                 if (hv_pf() && !mma) hv_prefetch(o, "chunk0 + " + S(nblocks));
             }
         }
-        std::vector<std::vector<bool>> done(ppt, std::vector<bool>(std::max(1, nblocks), false));
+        // a full group (every group but perhaps the last) runs its steps
+        // without the per-step bound check: forward CUDA-core kernels on
+        // Sobol points.  (Measured on GB300: FP32 GBM 1.13 -> 1.08 ms on XOR
+        // scrambles and 4.80 -> 4.44 ms shifted, Heston XOR unchanged; the
+        // ChaCha8 kernels and the batched kernel, which carries every
+        // template, slowed with the larger code: batched 54.5 -> 60.4 ms)
+        const bool full_copy = !mma && U > 1 && mode == Mode::Forward && sp.rng == RNG_SOBOL;
+        const std::vector<std::vector<bool>> done0(ppt, std::vector<bool>(std::max(1, nblocks), false));
+        for (int copy = full_copy ? 0 : 1; copy < 2; ++copy) {
+        if (full_copy) o.l(copy == 0 ? "if (t0 + " + S(U) + " <= n_steps) {" : "} else {");
+        std::vector<std::vector<bool>> done = done0;
         for (int g = 0; g < U; ++g) {
             o.l("{ const int t = t0 + " + S(g) + ";");
-            o.l("if (t < n_steps) {");
+            o.l(copy == 0 ? "{" : "if (t < n_steps) {");
             o.ind++;
             step_header(o);
             for (int j = 0; j < ppt; ++j) {
@@ -1133,6 +1143,8 @@ struct Gen {
             o.ind--;
             o.l("} }");
         }
+        }
+        if (full_copy) o.l("}");
         o.ind--;
         o.l("}");
         lane(0);
