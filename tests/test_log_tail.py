@@ -111,3 +111,20 @@ def test_outside_the_tail_range_uses_the_library_log(lib):
     with np.errstate(divide="ignore"):
         assert np.array_equal(_eval(lib, x), np.log(x))
     assert np.isnan(_eval(lib, np.array([-1.0, np.nan]))).all()
+
+
+def test_tables_are_the_generators():
+    """The tables in sde_log.h are what gen_log_table.py computes (mpmath)."""
+    pytest.importorskip("mpmath")
+    import io
+    import contextlib
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen_log_table", os.path.join(HEADER_DIR, "gen_log_table.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        gen.main()
+    with open(os.path.join(HEADER_DIR, "sde_log.h")) as f:
+        header = f.read()
+    assert buf.getvalue().strip() in header
