@@ -65,7 +65,7 @@ def _points(n, seed):
 
 
 def test_error_below_0_52_ulp(lib):
-    import mpmath
+    mpmath = pytest.importorskip("mpmath")
     mpmath.mp.dps = 60
     x = _points(12000, 1)
     y = _eval(lib, x)
