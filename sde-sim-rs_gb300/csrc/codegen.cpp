@@ -450,8 +450,12 @@ struct Gen {
             for (size_t i = 0; i + 1 < ks.size(); i += 2) {
                 const int ka = ks[i], kb = ks[i + 1];
                 const std::string pr = V("wp" + S(ka) + "_", kb);
-                const std::string src = xorm() ? "sde_normal_xor2(" + V("y", ka) + ", " + V("y", kb) + ")"
-                                                : "sde_normal_u53_2(" + V("U", ka) + ", " + V("U", kb) + ")";
+                // one reciprocal for the pair where the SFU pipe is the
+                // bound (the CUDA-core kernels); one each in the tensor-core
+                // step, which is bound by issue (measured both ways)
+                const std::string tpl = mma ? "<false>(" : "(";
+                const std::string src = xorm() ? "sde_normal_xor2" + tpl + V("y", ka) + ", " + V("y", kb) + ")"
+                                                : "sde_normal_u53_2" + tpl + V("U", ka) + ", " + V("U", kb) + ")";
                 o.l("const float2 " + pr + " = __fmul2_rn(make_float2(" + mult + ", " + mult + "), " + src + ");");
                 o.l("const float " + V("w", ka) + " = " + pr + ".x;");
                 o.l("const float " + V("w", kb) + " = " + pr + ".y;");

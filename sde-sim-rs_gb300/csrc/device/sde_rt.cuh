@@ -192,9 +192,14 @@ SDE_DEV float sde_normal_xor(sde_u32 y) {
 }
 
 /* Two normals at once: the polynomial and scaling work of both runs as
- * paired FP32 operations (one fma.f32x2 per pair of FMAs); the SFU work
- * (lg2, rsqrt, rcp) stays per element.  The numerator is formed negated so
- * the final step is a plain paired FMA. */
+ * paired FP32 operations (one fma.f32x2 per pair of FMAs); lg2 and rsqrt
+ * stay per element.  The two denominators share one reciprocal: both lie in
+ * [1, 28] (t <= 8.6 for q >= 2^-53), so r = 1/(den.x den.y) is far from
+ * overflow and 1/den.x = den.y r, 1/den.y = den.x r, about two ulp of 1/den
+ * against one for a reciprocal each, for one SFU operation fewer (SHARED;
+ * kernels not bound by the SFU pipe keep one each).  The numerator is
+ * formed negated so the final step is a plain paired FMA. */
+template <bool SHARED = true>
 SDE_DEV float2 sde_as26_abs2(float2 a) {
     const float2 r = make_float2(sde_rsqrt_approx(a.x), sde_rsqrt_approx(a.y));
     const float2 t = __fmul2_rn(a, r);
@@ -205,26 +210,34 @@ SDE_DEV float2 sde_as26_abs2(float2 a) {
                                                         make_float2(0.189269f, 0.189269f)),
                                              t, make_float2(1.432788f, 1.432788f)),
                                   t, make_float2(1.0f, 1.0f));
-    const float2 rc = make_float2(sde_rcp_approx(den.x), sde_rcp_approx(den.y));
+    float2 rc;
+    if (SHARED) {
+        const float rd = sde_rcp_approx(den.x * den.y);
+        rc = __fmul2_rn(make_float2(rd, rd), make_float2(den.y, den.x));
+    } else {
+        rc = make_float2(sde_rcp_approx(den.x), sde_rcp_approx(den.y));
+    }
     return __ffma2_rn(nnum, rc, t);
 }
 
+template <bool SHARED = true>
 SDE_DEV float2 sde_normal_xor2(sde_u32 ya, sde_u32 yb) {
     const sde_u32 sa = (sde_u32)((int)ya >> 31), sb = (sde_u32)((int)yb >> 31);
     const float2 lg = make_float2(sde_lg2_approx(__uint2float_rn(2u * (ya ^ sa) + 1u)),
                                   sde_lg2_approx(__uint2float_rn(2u * (yb ^ sb) + 1u)));
-    const float2 x = sde_as26_abs2(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
-                                              make_float2(45.747713916956393f, 45.747713916956393f)));
+    const float2 x = sde_as26_abs2<SHARED>(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
+                                                      make_float2(45.747713916956393f, 45.747713916956393f)));
     return make_float2(__int_as_float(__float_as_int(x.x) ^ (~sa & 0x80000000u)),
                        __int_as_float(__float_as_int(x.y) ^ (~sb & 0x80000000u)));
 }
 
+template <bool SHARED = true>
 SDE_DEV float2 sde_normal_u53_2(sde_u64 Ua, sde_u64 Ub) {
     const bool upa = Ua >= (1ull << 52), upb = Ub >= (1ull << 52);
     const sde_u64 Qa = upa ? (1ull << 53) - Ua : Ua, Qb = upb ? (1ull << 53) - Ub : Ub;
     const float2 lg = make_float2(sde_lg2_approx(__ull2float_rn(Qa)), sde_lg2_approx(__ull2float_rn(Qb)));
-    const float2 x = sde_as26_abs2(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
-                                              make_float2(73.473601139354201f, 73.473601139354201f)));
+    const float2 x = sde_as26_abs2<SHARED>(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
+                                                      make_float2(73.473601139354201f, 73.473601139354201f)));
     return make_float2(upa ? x.x : -x.x, upb ? x.y : -x.y);
 }
 
