@@ -40,8 +40,9 @@ STEPS_T = 256
 N_PATHS = 1 << 20
 REPS = 16
 SEED = 7
-# transcendental (SFU) operations per path-step as written: two normals
-# (log, sqrt, divide each) and sqrt(max(v, 0))
+# transcendental (SFU) operations per path-step of the formula as written:
+# two normals (log, sqrt, divide each) and sqrt(max(v, 0)); the algorithmic
+# count (the kernel issues 6: a pair of normals shares one reciprocal)
 SFU_PER_PATH_STEP = 7
 METRIC = "path-steps/s (fwd, Heston RQMC, FP32 stepping)"
 WORKLOAD = "heston_rqmc_sobol_xor_2^20x16_256steps"
