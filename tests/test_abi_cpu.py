@@ -297,3 +297,26 @@ def test_paths_per_thread_lowering(engine, ppt):
     N.check(N.lib().sde_plan_create(N.cstrs(["dX = (0.1 * X) * dW1"]), 1, N.cstrs([]), 0, N.cstrs(["X"]), 1,
                                     C.byref(opts), C.byref(h)))
     N.lib().sde_plan_destroy(h)
+
+
+def test_lowering_choices_of_the_measured_variants(engine):
+    """Each kernel family carries the variant measured faster on GB300:
+    * tensor-core XOR step: LO words bulk-copied (cp.async.bulk + mbarrier
+      expect_tx) into two buffers, drained on an early exit; Sobol high parts
+      by the unrolled loader; one reciprocal per normal;
+    * CUDA-core XOR kernels: high parts by set bits; a pair of normals
+      shares one reciprocal; full step groups without the bound check;
+    * ChaCha8 kernels: one copy of the step group (bound-checked)."""
+    from bench import basket_equations
+    eqs, pay, _, _ = basket_equations(16)
+    tc = engine.Plan(eqs, payoffs=[pay], rng="sobol", scramble="xor", precision="fp32", tensor_cores=True).source
+    assert "sde_bulk_g2s(" in tc and "sde_mbar_arrive_expect_tx(" in tc
+    assert "for (int s_ = lb_waited + 1; s_ <= lb_issued; ++s_)" in tc
+    assert "sde_sobol_hi_unrolled(" in tc and "sde_normal_xor2<false>(" in tc
+    fwd = engine.Plan(HESTON, payoffs=["max(S - 100, 0)"], rng="sobol", scramble="xor", precision="fp32",
+                      output="none").source
+    assert "= sde_sobol_hi(a.sobol_vt" in fwd and "sde_sobol_hi_unrolled(" not in fwd
+    assert "sde_normal_xor2(" in fwd and "<false>" not in fwd
+    assert "if (t0 + 16 <= n_steps) {" in fwd
+    pseudo = engine.Plan(GBM, payoffs=["X"], precision="fp32", output="none").source
+    assert "<= n_steps) {" not in pseudo and "if (t < n_steps) {" in pseudo
