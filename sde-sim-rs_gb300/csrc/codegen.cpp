@@ -1046,8 +1046,13 @@ struct Gen {
         if (mode == Mode::Forward) {
             o.l("const " + R + " tc = " + T("times") + ";");
             o.l("const " + R + " tn = " + T("times", "t + 1") + ";");
-            o.l("const " + R + " dt = " + T("dts") + ";");
-            o.l("const " + R + " sdt = " + T("sqrt_dts") + ";");
+            if (sp.ugrid && f32) {
+                o.l("const " + R + " dt = a.udt_f;");
+                o.l("const " + R + " sdt = a.usdt_f;");
+            } else {
+                o.l("const " + R + " dt = " + T("dts") + ";");
+                o.l("const " + R + " sdt = " + T("sqrt_dts") + ";");
+            }
         } else {
             o.l("const " + R + " tc = (" + R + ")t * bdt;");
             o.l("const " + R + " tn = (" + R + ")(t + 1) * bdt;");
@@ -1487,6 +1492,7 @@ static std::string tag(const KernelSpec& s) {
     if (s.icdf) r += "_acc";
     r += s.rng == RNG_PSEUDO ? "_pseudo" : (s.scramble == SCRAMBLE_XOR ? "_sobolxor" : "_sobolshift");
     if (s.ppt > 1) r += "_ppt" + std::to_string(s.ppt);
+    if (s.ugrid) r += "_ug";
     return r;
 }
 
@@ -1558,6 +1564,11 @@ KernelSpec wide_spec(const KernelSpec& s) {
     w.wide = false;
     return w;
 }
+KernelSpec wide_ugrid_spec(const KernelSpec& s) {
+    KernelSpec w = wide_spec(s);
+    w.ugrid = true;
+    return w;
+}
 
 std::string generate_source(const Universe& u, const KernelSpec& s) {
     Gen g(u, s);
@@ -1577,9 +1588,10 @@ std::string generate_source(const Universe& u, const KernelSpec& s) {
         src += "\n" + gc.forward_chunked(chunked_kernel_name(s));
     }
     if (has_wide_kernel(u, s)) {
-        const KernelSpec w = wide_spec(s);
-        Gen gw(u, w);
+        const KernelSpec w = wide_spec(s), wu = wide_ugrid_spec(s);
+        Gen gw(u, w), gu(u, wu);
         src += "\n" + gw.forward(forward_kernel_name(w));
+        src += "\n" + gu.forward(forward_kernel_name(wu));
     }
     if (s.adjoint) {
         KernelSpec s1 = s;

@@ -34,6 +34,8 @@ struct KernelSpec {
     int ckpt_every = 19;                // steps between adjoint checkpoints
     bool wide = false;                  // also build the two-paths-per-thread kernel
                                         // (where has_wide_kernel allows it)
+    bool ugrid = false;                 // FP32 dt and sqrt(dt) from the launch
+                                        // arguments (a grid of equal steps)
 };
 
 // Tensor-core lowering of correlated diffusions: eligible when the plan is
@@ -67,8 +69,11 @@ std::string chunked_kernel_name(const KernelSpec& s);
 // FP32 forward plans on XOR-scrambled Sobol with spec.wide set also carry
 // a kernel that steps two paths per thread in CTAs of 128 threads, for runs
 // with many paths; wide_spec is its specification.
+// It has a twin for grids whose FP32 steps are all equal, which takes dt and
+// sqrt(dt) from the launch arguments instead of loading them each step.
 bool has_wide_kernel(const Universe& u, const KernelSpec& s);
 KernelSpec wide_spec(const KernelSpec& s);
+KernelSpec wide_ugrid_spec(const KernelSpec& s);
 
 // CUDA C source of the kernels for one universe (without the runtime
 // header, which the JIT prepends).

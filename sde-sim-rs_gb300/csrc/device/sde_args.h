@@ -42,6 +42,8 @@ typedef struct sde_args {
     int ckpt_every;           /* adjoint: steps between checkpoints                  */
     int n_ckpt;               /* adjoint: checkpoints per path                       */
     int mask_stride;          /* words per replicate row of masks (multiple of 32)  */
+    float udt_f, usdt_f;      /* the FP32 step and its square root when every
+                                 step of the grid has them (uniform-grid kernels) */
     int pad1;
 } sde_args;
 

@@ -306,6 +306,7 @@ struct Loaded {
     cudaKernel_t adj = nullptr;
     cudaKernel_t chk = nullptr;  // chunked forward kernel for small runs
     cudaKernel_t wide = nullptr; // two paths per thread, for large runs
+    cudaKernel_t wide_ug = nullptr;  // the same on a grid of equal steps
 };
 
 // ---------------------------------------------------------------------------
@@ -324,6 +325,7 @@ struct sde_plan {
     int chunked = SDE_CHUNKED_AUTO;  // small runs: the chunked kernel (when built)
     std::string chk_name;            // empty: the plan has no chunked kernel
     std::string wide_name;           // empty: the plan has no two-paths-per-thread kernel
+    std::string wide_ug_name;        // its uniform-grid twin
     std::string source;
     std::string fwd_name, adj_name;
     std::shared_ptr<sde::Cubin> cubin;
@@ -389,8 +391,10 @@ static Loaded& ensure_loaded(sde_plan* p) {
             cuda_check(cudaLibraryGetKernel(&L.adj, L.lib, p->adj_name.c_str()), "cudaLibraryGetKernel");
         if (!p->chk_name.empty())
             cuda_check(cudaLibraryGetKernel(&L.chk, L.lib, p->chk_name.c_str()), "cudaLibraryGetKernel");
-        if (!p->wide_name.empty())
+        if (!p->wide_name.empty()) {
             cuda_check(cudaLibraryGetKernel(&L.wide, L.lib, p->wide_name.c_str()), "cudaLibraryGetKernel");
+            cuda_check(cudaLibraryGetKernel(&L.wide_ug, L.lib, p->wide_ug_name.c_str()), "cudaLibraryGetKernel");
+        }
     }
     return L;
 }
@@ -478,7 +482,10 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
     p->fwd_name = forward_kernel_name(p->spec);
     p->adj_name = adjoint_kernel_name(p->spec);
     if (has_chunked_kernel(p->u, p->spec) && p->chunked != SDE_CHUNKED_OFF) p->chk_name = chunked_kernel_name(p->spec);
-    if (has_wide_kernel(p->u, p->spec)) p->wide_name = forward_kernel_name(wide_spec(p->spec));
+    if (has_wide_kernel(p->u, p->spec)) {
+        p->wide_name = forward_kernel_name(wide_spec(p->spec));
+        p->wide_ug_name = forward_kernel_name(wide_ugrid_spec(p->spec));
+    }
     p->source = generate_source(p->u, p->spec);
     p->cubin = compile_cubin(p->source, p->spec.precision == PREC_FP32);
     return p.release();
@@ -596,11 +603,13 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         h_times_f[t] = (float)a.times[t];
         h_tidx[t] = -1;
     }
+    bool ugrid = T > 1;  // every FP32 step and its square root equal
     for (int t = 0; t + 1 < T; ++t) {
         h_dts[t] = a.times[t + 1] - a.times[t];
         h_sdts[t] = std::sqrt(a.times[t + 1] - a.times[t]);
         h_dts_f[t] = (float)h_dts[t];
         h_sdts_f[t] = (float)h_sdts[t];
+        ugrid = ugrid && h_dts_f[t] == h_dts_f[0] && h_sdts_f[t] == h_sdts_f[0];
     }
     for (int q = 0; q < std::max(1, P); ++q) h_x0[q] = (a.x0 && q < a.n_x0) ? a.x0[q] : 0.0;
     for (size_t k = 0; k < u.params.size(); ++k) h_par[k] = a.params[k];
@@ -627,6 +636,10 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     A.T = T;
     A.n_out = r->n_out;
     A.n_rep = a.n_replicates;
+    if (ugrid) {
+        A.udt_f = h_dts_f[0];
+        A.usdt_f = h_sdts_f[0];
+    }
 
     if (sobol) {
         SobolTables& st = sobol_tables(r->stream);
@@ -699,7 +712,8 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         r->block = block;
         r->per_block = (int)per_block;
         void* kargs[] = {&A};
-        cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : use_chk ? L.chk : use_wide ? L.wide : L.fwd),
+        cuda_check(cudaLaunchKernel((const void*)(p->spec.adjoint ? L.adj : use_chk ? L.chk
+                                                  : use_wide ? (ugrid ? L.wide_ug : L.wide) : L.fwd),
                                     dim3((unsigned)gx, (unsigned)a.n_replicates), dim3(block), kargs,
                                     tc ? (size_t)p->mma_smem : 0, r->stream),
                    "step kernel launch");

@@ -322,13 +322,17 @@ def test_automatic_wide_kernel(engine):
     """FP32 XOR-Sobol plans with automatic paths per thread launch the
     two-paths-per-thread kernel on large runs (here 2^16 paths x 16
     replicates) and the one-path kernel on small ones; both give the
-    filtration of a plan fixed at one path per thread, bit for bit."""
-    times = np.linspace(0.0, 1.0, 9)
+    filtration of a plan fixed at one path per thread, bit for bit.  On a
+    grid of equal steps the two-path kernel's twin takes dt and sqrt(dt)
+    from the launch arguments; an uneven grid runs the general one."""
+    uniform = np.linspace(0.0, 1.0, 9)
+    uneven = np.cumsum(np.concatenate([[0.0], np.random.default_rng(4).uniform(0.05, 0.2, 8)]))
     init = {"S": 100.0, "v": 0.04}
     kw = dict(rng="sobol", scramble="xor", precision="fp32", payoffs=["max(S - 100, 0)"], output="terminal")
     auto = engine.Plan(HESTON, **kw)
     one = engine.Plan(HESTON, paths_per_thread=1, **kw)
-    for n, reps, kernel in [((1 << 16) - 3, 16, "wide"), (5000, 2, "forward")]:
+    for times, n, reps, kernel in [(uniform, (1 << 16) - 3, 16, "wide"), (uneven, (1 << 16) - 3, 16, "wide"),
+                                   (uniform, 5000, 2, "forward")]:
         a = auto.run(times, init, n, seed=9, replicates=reps)
         b = one.run(times, init, n, seed=9, replicates=reps)
         info = a.launch_info()
