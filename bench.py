@@ -346,9 +346,9 @@ def run_engine(args):
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
-                         # ncu (1 pass, full size): 358.9 KB DRAM read (the Sobol
+                         # ncu (1 pass, full size): 490.5 KB DRAM read (the Sobol
                          # tables and masks), 0 B written
-                         "traffic": 358.91e3,
+                         "traffic": 490.5e3,
                          "traffic_source": "profiles/sde_step_euler_fp32_sobolxor_heston_rqmc.md (full-size capture)",
                          "peak_source": "measured by sde_probe_sfu_peak (MUFU throughput probe)",
                          "algorithmic_ops_per_launch": sfu_ops},
