@@ -19,51 +19,12 @@
 #include "sde_log.h"
 #endif
 
-/* ------------------------------------------------------------------------
- * ChaCha8 per scenario (rand_chacha 0.9 as called at src/rng/pseudo.rs:18
- * and src/rng/sobol.rs:68): 32-byte key from rand_core's PCG32-based
- * seed_from_u64, 64-bit block counter in words 12-13 starting at 0,
- * stream 0 in words 14-15, 8 rounds.  u64 number k of the stream is words
- * 2k (low) and 2k+1 (high).
- * ---------------------------------------------------------------------- */
-
-SDE_DEV sde_u32 sde_rotl(sde_u32 x, int n) { return __funnelshift_l(x, x, n); }
-
-SDE_DEV void sde_seed_from_u64(sde_u64 s, sde_u32 k[8]) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        s = s * 6364136223846793005ull + 11634580027462260723ull;
-        const sde_u32 xs = (sde_u32)(((s >> 18) ^ s) >> 27);
-        const sde_u32 rot = (sde_u32)(s >> 59);
-        k[i] = __funnelshift_r(xs, xs, rot);
-    }
-}
-
-#define SDE_QR(a, b, c, d)                          \
-    a += b; d ^= a; d = sde_rotl(d, 16);            \
-    c += d; b ^= c; b = sde_rotl(b, 12);            \
-    a += b; d ^= a; d = sde_rotl(d, 8);             \
-    c += d; b ^= c; b = sde_rotl(b, 7);
-
-SDE_DEV void sde_chacha8_block(const sde_u32 k[8], sde_u64 ctr, sde_u32 o[16]) {
-    sde_u32 x0 = 0x61707865u, x1 = 0x3320646eu, x2 = 0x79622d32u, x3 = 0x6b206574u;
-    sde_u32 x4 = k[0], x5 = k[1], x6 = k[2], x7 = k[3];
-    sde_u32 x8 = k[4], x9 = k[5], x10 = k[6], x11 = k[7];
-    const sde_u32 c0 = (sde_u32)ctr, c1 = (sde_u32)(ctr >> 32);
-    sde_u32 x12 = c0, x13 = c1, x14 = 0u, x15 = 0u;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        SDE_QR(x0, x4, x8, x12) SDE_QR(x1, x5, x9, x13)
-        SDE_QR(x2, x6, x10, x14) SDE_QR(x3, x7, x11, x15)
-        SDE_QR(x0, x5, x10, x15) SDE_QR(x1, x6, x11, x12)
-        SDE_QR(x2, x7, x8, x13) SDE_QR(x3, x4, x9, x14)
-    }
-    o[0] = x0 + 0x61707865u; o[1] = x1 + 0x3320646eu;
-    o[2] = x2 + 0x79622d32u; o[3] = x3 + 0x6b206574u;
-    o[4] = x4 + k[0]; o[5] = x5 + k[1]; o[6] = x6 + k[2]; o[7] = x7 + k[3];
-    o[8] = x8 + k[4]; o[9] = x9 + k[5]; o[10] = x10 + k[6]; o[11] = x11 + k[7];
-    o[12] = x12 + c0; o[13] = x13 + c1; o[14] = x14; o[15] = x15;
-}
+/* ChaCha8 per scenario: sde_seed_from_u64, sde_chacha8_block and the
+ * stream-precomputed sde_chacha8_block_s (prepended to the lowered
+ * kernels' source, included here for the nvcc-built ones) */
+#ifndef SDE_CHACHA_H
+#include "sde_chacha.h"
+#endif
 
 SDE_DEV sde_u64 sde_pair(sde_u32 lo, sde_u32 hi) { return ((sde_u64)hi << 32) | (sde_u64)lo; }
 

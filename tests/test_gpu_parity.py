@@ -33,7 +33,8 @@ def close64(gpu, ref):
 @pytest.mark.parametrize("seed", [0, 42, 2**63 + 11, 2**64 - 1])
 def test_kat_chacha8_bit_exact(engine, oracle, seed):
     from sde_sim_rs import _native as N
-    for first, n in ((0, 1000), (12345, 333)):
+    # the last two cross block 2^32, where the counter's high word turns on
+    for first, n in ((0, 1000), (12345, 333), (2**35 - 4, 8), (2**40 + 3, 64)):
         out = np.zeros(n, dtype=np.uint64)
         N.check(N.lib().sde_kat_chacha8_u64(seed, first, n, out.ctypes.data))
         assert np.array_equal(out, oracle.chacha8_u64(seed, first, n))
