@@ -270,6 +270,15 @@ def test_wide_kernel_lowering(engine):
     src = engine.Plan(HESTON, precision="fp32", rng="sobol", scramble="xor").source
     assert wide in src and "sde_step_euler_fp32_sobolxor(const sde_args a)" in src
     assert "__launch_bounds__(128) sde_step_euler_fp32_sobolxor_ppt2" in src
+    # its twin for grids of equal steps takes dt and sqrt(dt) from the
+    # argument block and reads neither per-step table
+    ug = src[src.index("sde_step_euler_fp32_sobolxor_ppt2_ug(const sde_args a)"):]
+    assert "__launch_bounds__(128) sde_step_euler_fp32_sobolxor_ppt2_ug" in src
+    assert "const float dt = a.udt_f;" in ug and "const float sdt = a.usdt_f;" in ug
+    assert "a.dts_f[" not in ug and "a.sqrt_dts_f[" not in ug
+    general = src[src.index("sde_step_euler_fp32_sobolxor_ppt2(const sde_args a)"):
+                  src.index("sde_step_euler_fp32_sobolxor_ppt2_ug(const sde_args a)")]
+    assert "a.dts_f[" in general and "a.udt_f" not in general
     from bench import basket_equations
     for eqs, kw in [(HESTON, dict(paths_per_thread=1)), (HESTON, dict(block_size=256)),
                     (HESTON, dict(precision="fp64")), (HESTON, dict(scramble="shift")),
