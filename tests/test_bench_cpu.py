@@ -1,0 +1,40 @@
+"""bench.py's reference arm runs on the host cores alone: rank 0 prints one
+JSON line with the contract's keys, on the headline's metric and workload;
+other ranks print nothing and exit 0."""
+import json
+import os
+import subprocess
+import sys
+
+from conftest import ROOT
+
+ARGS = [sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3", "--cpu-paths", "2048"]
+KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+        "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e")
+
+
+def _run(env=None):
+    r = subprocess.run(ARGS, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+
+
+def test_reference_arm_line():
+    lines = _run()
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in KEYS:
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
+    assert d["unit"] == "path-steps/s" and d["e2e"]["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["value"] == d["value"] and cb["cores"] >= 1 and "2048 paths" in cb["sample"]
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["metric"] == bench.METRIC and d["config"]["workload"] == bench.WORKLOAD
+
+
+def test_reference_arm_other_ranks_print_nothing():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2")
+    assert _run(env) == []
