@@ -329,3 +329,41 @@ def test_lowering_choices_of_the_measured_variants(engine):
     assert "if (t0 + 16 <= n_steps) {" in fwd
     pseudo = engine.Plan(GBM, payoffs=["X"], precision="fp32", output="none").source
     assert "<= n_steps) {" not in pseudo and "if (t < n_steps) {" in pseudo
+
+
+def test_register_budgets_of_the_measured_kernels(engine):
+    """The kernels keep the register counts their measured occupancy rests
+    on (ptxas, as NVRTC compiles the plan), and none spills.  A lowering
+    change that crosses a budget moves the kernel to another occupancy class
+    and needs measuring again."""
+    from bench import PAYOFF, basket_equations
+    eqs, pay, _, _ = basket_equations(64)
+    budgets = {
+        "sde_step_euler_fp32_sobolxor_ppt2_ug": 48,   # Heston RQMC headline, CTAs of 128
+        "sde_step_euler_fp32_sobolxor_ppt2": 56,
+        "sde_step_euler_fp32_sobolxor": 32,           # one path per thread, CTAs of 256
+        "sde_step_euler_fp32_sobolshift": 64,
+        "sde_step_euler_fp64_pseudo_chunked": 64,
+        "sde_step_euler_fp64_pseudo": 64,
+        "sde_step_euler_fp32_sobolxor_tc": 80,
+        "sde_adjoint_euler_fp32_pseudo": 40,
+        "sde_step_euler_fp32_pseudo": 40,
+    }
+    plans = [
+        engine.Plan(HESTON, payoffs=[PAYOFF], rng="sobol", scramble="xor", precision="fp32", output="none"),
+        engine.Plan(HESTON, payoffs=[PAYOFF], rng="sobol", scramble="shift", precision="fp32", output="none"),
+        engine.Plan(GBM, precision="fp64"),
+        engine.Plan(eqs, payoffs=[pay], rng="sobol", scramble="xor", precision="fp32", tensor_cores=True,
+                    output="none"),
+        engine.Plan(GBM, payoffs=["max(X - 1, 0)"], grad_x0=["X"], precision="fp32", output="none"),
+    ]
+    seen = {}
+    for p in plans:
+        for m in re.finditer(r"Function properties for (\w+)\n.*?(\d+) bytes spill stores.*?\n"
+                             r"ptxas info    : Used (\d+) registers", p.compile_log, re.S):
+            seen[m.group(1)] = (int(m.group(2)), int(m.group(3)))
+    assert set(budgets) <= set(seen), set(budgets) - set(seen)
+    for name, cap in budgets.items():
+        spill, regs = seen[name]
+        assert spill == 0, name
+        assert regs <= cap, (name, regs, cap)
