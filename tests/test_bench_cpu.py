@@ -1,8 +1,10 @@
 """bench.py's reference arm runs on the host cores alone: rank 0 prints one
 JSON line with the contract's keys, on the headline's metric and workload;
-other ranks print nothing and exit 0."""
+other ranks print nothing and exit 0.  The ncu summaries under profiles/
+give commands that run committed files with the clocks left unlocked."""
 import json
 import os
+import re
 import subprocess
 import sys
 
@@ -38,3 +40,19 @@ def test_reference_arm_line():
 def test_reference_arm_other_ranks_print_nothing():
     env = dict(os.environ, RANK="1", WORLD_SIZE="2")
     assert _run(env) == []
+
+
+def test_profile_summaries_cite_committed_commands():
+    """Each ncu summary gives the command that made it: every ncu line keeps
+    the clocks unlocked, and every script it runs is a committed file."""
+    d = os.path.join(ROOT, "profiles")
+    names = sorted(n for n in os.listdir(d) if n.endswith((".md", ".txt")))
+    assert names
+    for n in names:
+        with open(os.path.join(d, n)) as f:
+            text = f.read()
+        ncu = [ln for ln in text.splitlines() if re.match(r"\s*ncu ", ln)]
+        assert ncu, n
+        assert all("--clock-control none" in ln for ln in ncu), n
+        for script in set(re.findall(r"python ([\w/.-]+\.py)", text)):
+            assert os.path.isfile(os.path.join(ROOT, script)) and not script.startswith("_work"), (n, script)
