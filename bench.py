@@ -178,17 +178,42 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm), "interval_ms": self.INTERVAL_MS}
 
 
-def cpu_sample(threads: int, paths: int):
+# The oracle's RNG modes: the bench's XOR replicates (not a reference mode),
+# the reference's own Sobol mode (point s+5 shifted by the scenario's ChaCha8
+# doubles, src/rng/sobol.rs:35-79) and its default pseudo-random mode
+# (ChaCha8 per scenario, src/rng/pseudo.rs:14-31).
+CPU_MODES = ("sobol_xor", "sobol_shift", "pseudo")
+
+
+def cpu_sample(threads: int, paths: int, mode: str = "sobol_xor"):
     """Time the oracle on `paths` paths of replicate 0 (FP64, same equations,
-    same scrambled Sobol inputs).  Returns (path-steps/s, seconds)."""
+    same random inputs as the GPU arm in the XOR mode).  Returns
+    (path-steps/s, seconds)."""
     from oracle import oracle as O
     O.build()
     u = O.Universe(HESTON)
+    rng, scr = {"sobol_xor": (O.SOBOL, O.XOR), "sobol_shift": (O.SOBOL, O.SHIFT),
+                "pseudo": (O.PSEUDO, O.SHIFT)}[mode]
     t0 = time.perf_counter()
-    u.estimate(times(), INIT, 0, paths, PAYOFF, rng=O.SOBOL, scramble=O.XOR, seed=SEED,
+    u.estimate(times(), INIT, 0, paths, PAYOFF, rng=rng, scramble=scr, seed=SEED,
                n_per_replicate=N_PATHS, threads=threads)
     dt = time.perf_counter() - t0
     return paths * STEPS_T / dt, dt
+
+
+def cpu_rate(threads: int, paths: int, warmup: int, samples: int, mode: str = "sobol_xor"):
+    """Warmed median of the oracle's throughput: `warmup` untimed runs on a
+    sixteenth of the sample (library load, Sobol tables, thread start-up),
+    then the median of `samples` timed runs.  Both arms use this sampler."""
+    for _ in range(max(1, warmup)):
+        cpu_sample(threads, max(1024, paths // 16), mode)
+    vals = [cpu_sample(threads, paths, mode)[0] for _ in range(max(1, samples))]
+    return statistics.median(vals)
+
+
+def cpu_modes(threads: int, paths: int, samples: int = 3):
+    """The oracle's rate in the reference's own RNG modes beside the XOR one."""
+    return {m: cpu_rate(threads, paths, 1, samples, m) for m in CPU_MODES if m != "sobol_xor"}
 
 
 def run_reference(args):
@@ -197,13 +222,7 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     paths = args.cpu_paths
-    for _ in range(args.warmup):
-        cpu_sample(threads, max(1024, paths // 16))
-    vals = []
-    for _ in range(args.steps):
-        v, _ = cpu_sample(threads, paths)
-        vals.append(v)
-    value = statistics.median(vals)
+    value = cpu_rate(threads, paths, args.warmup, args.steps)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "path-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": paths * STEPS_T / value * 1e3, "higher_is_better": True,
@@ -213,10 +232,27 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{paths} paths x {STEPS_T} steps of replicate 0 per step "
                                        "(CPU restatement of the sde-sim-rs algorithm, FP64; the Rust "
-                                       "reference cannot be built on this host)"},
+                                       "reference cannot be built on this host)",
+                             "reference_modes": cpu_modes(threads, paths, min(3, args.steps)),
+                             "note": "value: the XOR-scrambled Sobol inputs of the GPU arm; reference_modes: "
+                                     "the same sample in the reference's own Sobol (shifted point s+5) and "
+                                     "pseudo-random (ChaCha8) modes"},
             "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def equal_rmse_speedup(thr32: float, thr64: float, bias: float, se: float):
+    """Throughput ratio at equal estimator RMSE.  With RMSE^2 = se^2 N / N'
+    + bias^2 (se: the FP64 estimator's standard error at N paths; bias: the
+    FP32 estimate minus the FP64 one on the same random inputs), FP32 needs
+    N' = N se^2 / (se^2 - bias^2) paths to match the FP64 RMSE at N, so the
+    time ratio is (thr32 / thr64) (1 - bias^2 / se^2); 0 when the bias alone
+    exceeds the FP64 error."""
+    if not (se > 0 and math.isfinite(se)):
+        return None
+    f = 1.0 - (bias / se) ** 2
+    return thr32 / thr64 * f if f > 0 else 0.0
 
 
 def run_engine(args):
@@ -295,30 +331,36 @@ def run_engine(args):
                  "ms": statistics.median(ms_sh), "estimate": sh_price,
                  "note": "the reference's Sobol mode: point s+5, ChaCha8 shift per scenario and dimension"}
 
-    # the plain FP64 GPU path on the same scrambled inputs (a sample of the
-    # paths): its throughput and the FP32 estimate's deviation from it
+    # the plain FP64 GPU path on the same scrambled inputs at the same size
+    # (2^20 paths x 16 replicates), warmed and L2-flushed like the FP32 leg:
+    # its throughput, the FP32 estimate's deviation from it, and the speedup
+    # at equal RMSE with the RQMC standard error at full size
     fp64 = None
     if args.fp64_paths:
         p64 = sde_sim_rs.Plan(HESTON, payoffs=[PAYOFF], rng="sobol", scramble="xor", precision="fp64",
                               output="none")
-        n64 = args.fp64_paths
+        n64 = min(args.fp64_paths, npaths)
         one(p64, n64).estimates()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        r64 = one(p64, n64)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ms64 = e0.elapsed_time(e1)
-        r32 = one(plan, n64)
-        m64 = r64.estimates()[0][:, 0] / n64
-        m32 = r32.estimates()[0][:, 0] / n64
-        v64 = n64 * reps * STEPS_T / (ms64 * 1e-3)
-        bias = float(np.abs(m32 - m64).max())
+        ms64, r64 = _timed_runs(lambda: one(p64, n64), 2, stream, flush)
+        m64 = r64[-1].estimates()[0][:, 0] / n64
+        m32 = (sums / npaths if n64 == npaths else one(plan, n64).estimates()[0][:, 0] / n64)
+        v64 = n64 * reps * STEPS_T / (statistics.median(ms64) * 1e-3)
+        bias = float(np.mean(m32 - m64))
         se64 = float(m64.std(ddof=1) / math.sqrt(reps))
-        fp64 = {"value": v64, "unit": "path-steps/s", "sample": f"{n64} paths x {reps} replicates",
+        fp64 = {"value": v64, "unit": "path-steps/s", "ms": statistics.median(ms64),
+                "sample": f"{n64} paths x {reps} replicates (the FP32 leg's size)" if n64 == npaths
+                else f"{n64} paths x {reps} replicates",
                 "estimate": float(m64.mean()),
-                "fp32_minus_fp64_max_abs_per_replicate": bias, "rqmc_se_at_sample": se64,
-                "equal_rmse_speedup": value / v64 * (1.0 if bias < se64 else (se64 / bias) ** 2)}
+                "fp32_minus_fp64": bias,
+                "fp32_minus_fp64_max_abs_per_replicate": float(np.abs(m32 - m64).max()),
+                "rqmc_se": se64,
+                "equal_rmse_speedup": equal_rmse_speedup(value / world, v64, bias, se64),
+                "model": "RMSE^2 = se^2 N/N' + bias^2, se of the FP64 RQMC estimate at this size"}
+
+    # the metric's forward+adjoint half: pathwise Greeks of GBM and Heston,
+    # 2^20 paths x 365 steps, FP32 forward + reverse sweep, against the plain
+    # FP64 GPU forward at the same size
+    adjoint = adjoint_legs(args, stream, flush, min(npaths, 1 << 20)) if args.adjoint else None
 
     # roofline: SFU bound; peak measured by a MUFU throughput probe
     peak = C.c_double()
@@ -327,7 +369,9 @@ def run_engine(args):
     achieved = sfu_ops / (ms_step * 1e-3)
 
     if rank == 0:
-        cpu_v, cpu_s = cpu_sample(os.cpu_count() or 1, args.cpu_paths) if args.cpu_baseline else (None, 0)
+        threads = os.cpu_count() or 1
+        cpu_v = cpu_rate(threads, args.cpu_paths, 1, 3) if args.cpu_baseline else None
+        cpu_m = cpu_modes(threads, args.cpu_paths) if args.cpu_baseline else None
         line = {
             "metric": METRIC, "value": value, "unit": "path-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -343,6 +387,7 @@ def run_engine(args):
                     "d2h_bytes_per_step": reps * 16},
             "fp64_gpu": fp64,
             "sobol_shift_fp32": shift_leg,
+            "fwd_adjoint": adjoint,
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
@@ -352,10 +397,11 @@ def run_engine(args):
                          "traffic_source": "profiles/sde_step_euler_fp32_sobolxor_heston_rqmc.md (full-size capture)",
                          "peak_source": "measured by sde_probe_sfu_peak (MUFU throughput probe)",
                          "algorithmic_ops_per_launch": sfu_ops},
-            "cpu_baseline": {"value": cpu_v, "unit": "path-steps/s", "cores": os.cpu_count(),
+            "cpu_baseline": {"value": cpu_v, "unit": "path-steps/s", "cores": threads,
                              "kind": "port",
                              "sample": f"{args.cpu_paths} paths x {STEPS_T} steps of replicate 0, FP64 "
-                                       f"oracle ({cpu_s:.1f} s)"},
+                                       "oracle, median of 3 after a warm-up (the reference arm's sampler)",
+                             "reference_modes": cpu_m},
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -563,12 +609,31 @@ def run_basket(args):
     for _ in range(2):
         one().estimates()
     e2e_s = (time.perf_counter() - t0) / 2
+    # the basket price's error against FP64 on the same inputs: the plain FP64
+    # GPU plan on the first n_s paths (XOR points 0..n_s-1, the timed run's
+    # first paths), each FP32 leg on the same paths, per-path payoff
+    # differences; and against the FP64 oracle on the CPU sample below
+    n_s = min(n, 1 << 17)
+    p64 = sde_sim_rs.Plan(eqs, rng="sobol", scramble="xor", precision="fp64", output="terminal")
+    x64 = p64.run(T, init, n_s, seed=7, stream=stream).values()[0, :, -1, :]
+    pay = lambda x: np.maximum(x.sum(axis=1) / 64 - 100.0, 0.0)
+    pay64 = pay(x64)
+    for v in legs.values():
+        x32 = v["plan"].run(T, init, n_s, seed=7, checkpoints=[128], stream=stream).values()[0, :, -1, :]
+        d = pay(x32) - pay64
+        v["price_minus_fp64"] = float(d.mean())
+        v["price_minus_fp64_se"] = float(d.std(ddof=1) / math.sqrt(n_s))
+        v["max_abs_rel_terminal_vs_fp64"] = float(np.max(np.abs(x32 - x64) / np.abs(x64)))
+        v["x32_head"] = x32[:512]
     u = O.Universe(eqs)
     cpu_n = 512
     c0 = time.perf_counter()
-    u.estimate(T, {f"S{i + 1}": 100.0 for i in range(64)}, 0, cpu_n, payoff, rng=O.SOBOL, scramble=O.XOR,
-               seed=7, n_per_replicate=n, threads=os.cpu_count() or 1)
+    xo = u.simulate(T, init, 0, cpu_n, rng=O.SOBOL, scramble=O.XOR, seed=7, n_per_replicate=n, full=False,
+                    threads=os.cpu_count() or 1)
     cpu_s = time.perf_counter() - c0
+    oracle_err = {k: {"price_minus_oracle": float((pay(v["x32_head"]) - pay(xo)).mean()),
+                      "max_abs_rel_terminal_vs_oracle": float(np.max(np.abs(v.pop("x32_head") - xo) / np.abs(xo)))}
+                  for k, v in legs.items()}
     _common(args, "basket64_euler_fp32_sobolxor_2^21x128_32ckpt", "path-steps/s (fwd, 64-dim basket, FP32)",
             ps / (ms_step * 1e-3), ms_step, "f32", clk.summary(),
             {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 129 * 28 + 64 * 8,
@@ -582,11 +647,17 @@ def run_basket(args):
              "traffic_source": "profiles/sde_step_basket64_tc_fp16.md (full-size capture)",
              "bytes_written_per_launch": nbytes},
             {"value": cpu_n * 128 / cpu_s, "unit": "path-steps/s", "cores": os.cpu_count(), "kind": "port",
-             "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, estimator only"},
+             "sample": f"{cpu_n} paths x 128 steps, FP64 oracle, terminal values"},
             {"paths": n, "steps": 128, "checkpoints": 32, "price": price, "price_se": se,
+             "price_minus_fp64": main_leg["price_minus_fp64"], "price_minus_fp64_se": main_leg["price_minus_fp64_se"],
+             "fp64_error_sample": f"FP64 GPU plan on the first {n_s} paths (same XOR points), per-path payoff "
+                                  f"differences; oracle: the first {cpu_n} paths",
+             "oracle_error": oracle_err,
              "roofline_compute": compute,
              "kernel": "tcgen05 (3 x FP16 split, FP32 accumulate)" if main_leg["tc"] else "CUDA cores",
              "legs": {k: {"ms": v["ms"], "path_steps_per_s": ps / (v["ms"] * 1e-3), "price": v["price"],
+                          "price_minus_fp64": v["price_minus_fp64"], "price_minus_fp64_se": v["price_minus_fp64_se"],
+                          "max_abs_rel_terminal_vs_fp64": v["max_abs_rel_terminal_vs_fp64"],
                           "tensor_cores": v["tc"]} for k, v in legs.items()}})
 
 
@@ -654,24 +725,29 @@ def run_batched(args):
              "fraction_within_3se_of_fp64": float(np.mean(z < 3)), "max_z": float(z.max())})
 
 
-def run_adjoint(args):
-    """Pathwise adjoint Greeks, 2^20 paths, 365 steps, FP32 forward + reverse,
-    checkpoints every 19 steps, against the plain FP64 GPU forward pass."""
+ADJ_MODELS = (
+    ("gbm", GBM_P, {"mu": 0.05, "sigma": 0.2}, ["mu", "sigma"], ["X"], {"X": 100.0}, "max(X - 100, 0)"),
+    ("heston", HESTON_P, {"kappa": 2.0, "theta": 0.04, "xi": 0.3, "rho": -0.7, "mu": 0.03},
+     ["kappa", "theta", "xi", "rho"], ["v"], {"S": 100.0, "v": 0.04}, "max(S - 100, 0)"))
+ADJ_STEPS = 365
+
+
+def adjoint_legs(args, stream, flush, n, scheme="euler"):
+    """Pathwise Greeks of GBM (d/d mu, sigma, X0) and Heston (d/d kappa,
+    theta, xi, rho, v0): 2^20 pseudo-random paths x 365 steps, checkpoints
+    every 19 steps, FP32 forward + reverse sweep, L2 flushed between timed
+    launches.  Beside it, on the same paths (same seeds): the plain FP64 GPU
+    forward (timed the same way), and one FP64 adjoint run that gives every
+    FP32 estimate and gradient its error against FP64."""
     import numpy as np
-    import torch
     import sde_sim_rs
-    n = args.paths if args.paths != N_PATHS else 1 << 20
-    T = np.linspace(0.0, 1.0, 366)
-    stream = torch.cuda.current_stream()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    T = np.linspace(0.0, 1.0, ADJ_STEPS + 1)
     out = {}
-    for name, eqs, params, gp, gx, init, pay in (
-            ("gbm", GBM_P, {"mu": 0.05, "sigma": 0.2}, ["mu", "sigma"], ["X"], {"X": 100.0}, "max(X - 100, 0)"),
-            ("heston", HESTON_P, {"kappa": 2.0, "theta": 0.04, "xi": 0.3, "rho": -0.7, "mu": 0.03},
-             ["kappa", "theta", "xi", "rho"], ["v"], {"S": 100.0, "v": 0.04}, "max(S - 100, 0)")):
-        adj = sde_sim_rs.Plan(eqs, params=list(params), payoffs=[pay], grad_params=gp, grad_x0=gx,
-                              precision="fp32", output="none")
-        f64 = sde_sim_rs.Plan(eqs, params=list(params), payoffs=[pay], precision="fp64", output="none")
+    for name, eqs, params, gp, gx, init, pay in ADJ_MODELS:
+        kw = dict(params=list(params), payoffs=[pay], scheme=scheme, output="none")
+        adj = sde_sim_rs.Plan(eqs, grad_params=gp, grad_x0=gx, precision="fp32", **kw)
+        f64 = sde_sim_rs.Plan(eqs, precision="fp64", **kw)
+        a64 = sde_sim_rs.Plan(eqs, grad_params=gp, grad_x0=gx, precision="fp64", **kw)
         one_a = lambda: adj.run(T, init, n, seed=42, params=params, stream=stream)
         one_f = lambda: f64.run(T, init, n, seed=42, params=params, stream=stream)
         for _ in range(args.warmup):
@@ -692,23 +768,47 @@ def run_adjoint(args):
         m = s[0] / n
         se = np.sqrt(np.maximum(q[0] / n - m * m, 0) / n)
         s64, q64 = rf[-1].estimates()
-        ta, tf = sum(ms_a) / len(ms_a), sum(ms_f) / len(ms_f)
-        out[name] = {"fwd_adjoint_path_steps_per_s": n * 365 / (ta * 1e-3),
-                     "fp64_fwd_path_steps_per_s": n * 365 / (tf * 1e-3),
-                     "speedup_fp32_fwd_adj_vs_fp64_fwd": tf / ta,
-                     "price_fp32": float(m[0]), "price_fp64": float(s64[0, 0] / n), "price_se": float(se[0]),
-                     "gradients": dict(zip(gp + gx, [float(x) for x in m[1:]])),
-                     "gradient_se": dict(zip(gp + gx, [float(x) for x in se[1:]])), "ms": ta,
-                     "e2e_path_steps_per_s": n * 365 / statistics.median(e2e_t), "clk": clk.summary(),
-                     "kt": 1 + len(gp) + len(gx)}
+        p64 = float(s64[0, 0] / n)
+        se64 = float(math.sqrt(max(q64[0, 0] / n - p64 * p64, 0) / n))
+        g64 = a64.run(T, init, n, seed=42, params=params, stream=stream).estimates()[0][0] / n
+        ta, tf = statistics.median(ms_a), statistics.median(ms_f)
+        thr_a, thr_f = n * ADJ_STEPS / (ta * 1e-3), n * ADJ_STEPS / (tf * 1e-3)
+        names = gp + gx
+        out[name] = {"fwd_adjoint_path_steps_per_s": thr_a, "fp64_fwd_path_steps_per_s": thr_f,
+                     "throughput_ratio_fp32_fwd_adj_vs_fp64_fwd": thr_a / thr_f,
+                     "equal_rmse_speedup": equal_rmse_speedup(thr_a, thr_f, float(m[0]) - p64, se64),
+                     "price_fp32": float(m[0]), "price_fp64": p64, "price_se": se64,
+                     "price_fp32_minus_fp64": float(m[0]) - p64,
+                     "gradients": dict(zip(names, [float(x) for x in m[1:]])),
+                     "gradient_se": dict(zip(names, [float(x) for x in se[1:]])),
+                     "gradient_fp32_minus_fp64": dict(zip(names, [float(x) for x in (m[1:] - g64[1:])])),
+                     "ms": ta, "fp64_fwd_ms": tf,
+                     "e2e_path_steps_per_s": n * ADJ_STEPS / statistics.median(e2e_t),
+                     "clocks": clk.summary(), "n_estimates": 1 + len(names)}
+    out["config"] = {"paths": n, "steps": ADJ_STEPS, "ckpt_every": 19, "rng": "pseudo (ChaCha8)",
+                     "scheme": scheme, "l2": "flushed (256 MiB write) between timed launches",
+                     "model": "equal_rmse_speedup: RMSE^2 = se^2 N/N' + bias^2 with the FP64 forward's se "
+                              "at N and the FP32 price's bias against it on the same paths"}
+    return out
+
+
+def run_adjoint(args):
+    """Pathwise adjoint Greeks, 2^20 paths, 365 steps, FP32 forward + reverse,
+    checkpoints every 19 steps, against the plain FP64 GPU forward pass."""
+    import torch
+    n = args.paths if args.paths != N_PATHS else 1 << 20
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = adjoint_legs(args, stream, flush, n, scheme=args.scheme)
     g = out["gbm"]
-    clocks = g.pop("clk")
-    out["heston"].pop("clk")
-    h2d = (366 * 3 + 365 * 2) * 8 + 366 * (4 + 4) + 64
+    clocks = g.pop("clocks")
+    out["heston"].pop("clocks")
+    h2d = ((ADJ_STEPS + 1) * 3 + ADJ_STEPS * 2) * 8 + (ADJ_STEPS + 1) * (4 + 4) + 64
     e2e = {"value": g["e2e_path_steps_per_s"], "unit": "path-steps/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": g.pop("kt") * 16, "through": "Plan.run(...).estimates() (price and gradient sums)"}
-    out["heston"].pop("kt")
-    _common(args, "adjoint_gbm_heston_2^20x365", "path-steps/s (fwd+adjoint, GBM, FP32)",
+           "d2h_bytes_per_step": g.pop("n_estimates") * 16,
+           "through": "Plan.run(...).estimates() (price and gradient sums)"}
+    out["heston"].pop("n_estimates")
+    _common(args, f"adjoint_gbm_heston_2^20x365_{args.scheme}", f"path-steps/s (fwd+adjoint, GBM, FP32, {args.scheme})",
             g["fwd_adjoint_path_steps_per_s"], g["ms"], "f32", clocks, e2e, 2 * args.steps,
             _chacha_roofline(g["fwd_adjoint_path_steps_per_s"], 1.0 / 8.0,
                              "the forward pass draws one u64 per path-step; the reverse sweep reads the stored "
@@ -728,9 +828,14 @@ def main():
     ap.add_argument("--cpu-paths", type=int, default=1 << 17)
     ap.add_argument("--paths", type=int, default=N_PATHS)
     ap.add_argument("--reps", type=int, default=REPS)
-    ap.add_argument("--fp64-paths", type=int, default=1 << 14)
+    ap.add_argument("--fp64-paths", type=int, default=N_PATHS,
+                    help="heston_rqmc: paths per replicate of the FP64 GPU leg (default: the FP32 leg's)")
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
+                    help="heston_rqmc: leave out the fwd+adjoint legs")
+    ap.add_argument("--scheme", default="euler", choices=["euler", "runge-kutta"],
+                    help="adjoint: the scheme whose recursion the reverse sweep runs")
     ap.add_argument("--cuda-cores-only", action="store_true",
                     help="basket: time only the CUDA-core kernel (no tcgen05 leg)")
     ap.add_argument("--chunked", default="auto", choices=["auto", "on", "off"],

@@ -263,8 +263,11 @@ int sde_result_launch_info(const sde_result* r, int32_t* kernel, int32_t* block,
  * synchronous on stream.  A run needing more than 4 MiB of scratch (about
  * 5e5 blocks x payoffs x replicates) fails with SDE_ERR_INVALID.  The
  * first call on a device loads the plan's kernels and resolves the array's
- * address; make it before any stream capture.  Every call shares the
- * array: calls that overlap on the GPU (other streams, other threads) race. */
+ * address.  Every call copies from pageable host memory and synchronizes
+ * the stream, so none may be made on a stream under capture.  Every call
+ * shares the array: calls that overlap on the GPU (other streams, other
+ * threads) race.  A call that fails after queueing work waits for that work
+ * before it returns.                                                       */
 int sde_run_estimates_static(sde_plan* plan, const double* times, int32_t n_times,
                              const double* x0, int32_t n_x0, const double* params, int32_t n_params,
                              uint64_t n_paths, int32_t n_replicates, uint64_t seed, void* stream,

@@ -49,6 +49,11 @@ class _Cfg(C.Structure):
                 ("sobol_v", C.POINTER(C.c_uint32)), ("sobol_dims", C.c_int), ("icdf", C.c_int)]
 
 
+class _Jump(C.Structure):
+    _fields_ = [("t", C.c_int32), ("idx", C.c_int32), ("u", C.c_double), ("lam", C.c_double),
+                ("k", C.c_uint64)]
+
+
 _lib = None
 
 
@@ -91,6 +96,9 @@ def lib():
         L.orc_icdf_as26.restype = C.c_double
         L.orc_icdf_accurate.argtypes = [C.c_double]
         L.orc_icdf_accurate.restype = C.c_double
+        L.orc_jump_trace.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double),
+                                     C.c_uint64, C.POINTER(_Cfg), C.POINTER(_Jump), C.c_int,
+                                     C.POINTER(C.c_int), C.c_char_p, C.c_size_t]
         L.orc_poisson.argtypes = [C.c_double, C.c_double]
         L.orc_poisson.restype = C.c_uint64
         _lib = L
@@ -184,6 +192,27 @@ def icdf_as26(p: float) -> float:
 
 def poisson(u: float, lam: float) -> int:
     return int(lib().orc_poisson(u, lam))
+
+
+def poisson_boundary_ulps(u: float, lam: float) -> float:
+    """Distance, in units of the last place of u, from the uniform u to the
+    nearest cumulative probability F(k) that the reference's inversion walk
+    (src/proc/increment.rs:182-200) compares it with: F(0) = exp(-lam),
+    F(k) = F(k-1) + p(k-1) lam / k, up to one past the count it returns.  A
+    count that flips on a last-bit difference of lam (or of exp) has u
+    within a few units of the last place of one of them."""
+    import math
+    if lam <= 0.0:
+        return math.inf
+    k_end = poisson(u, lam) + 1
+    p = math.exp(-lam)
+    f = p
+    best = abs(u - f)
+    for k in range(1, min(k_end, 200) + 1):
+        p *= lam / k
+        f += p
+        best = min(best, abs(u - f))
+    return best / math.ulp(max(u, 1e-300))
 
 
 class Universe:
@@ -286,6 +315,26 @@ class Universe:
         if rc:
             raise OracleError(err.value.decode())
         return s.value, q.value
+
+    def jump_trace(self, times, initial_values, scenario, *, scheme=EULER, rng=PSEUDO, scramble=SHIFT,
+                   semantics=REFERENCE, seed=0, n_per_replicate=0, icdf=0, max_draws=0):
+        """Every Poisson draw of one scenario in draw order: a list of
+        (step, stochastic index, uniform, lambda * dt, count)."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        T = len(times)
+        x0 = self.x0(initial_values)
+        cfg = self._cfg(scheme, rng, scramble, semantics, seed, n_per_replicate or (scenario + 1),
+                        (T - 1) * self.n_stochastic, icdf)
+        max_draws = max_draws or 64 * max(1, T - 1)
+        buf = (_Jump * max_draws)()
+        n = C.c_int()
+        err = C.create_string_buffer(1024)
+        rc = lib().orc_jump_trace(self._h, times.ctypes.data_as(C.POINTER(C.c_double)), T,
+                                  x0.ctypes.data_as(C.POINTER(C.c_double)), scenario, C.byref(cfg), buf,
+                                  max_draws, C.byref(n), err, len(err))
+        if rc:
+            raise OracleError(err.value.decode())
+        return [(buf[i].t, buf[i].idx, buf[i].u, buf[i].lam, buf[i].k) for i in range(n.value)]
 
     def payoff(self, expr, t, rows):
         rows = np.ascontiguousarray(rows, dtype=np.float64)

@@ -899,6 +899,8 @@ typedef struct {
     double* step_vals;
     /* sobol */
     double* sobol_vals;  /* [(T-1)*n_inc] */
+    orc_jump* trace;     /* optional record of every Poisson draw */
+    int trace_max, trace_n;
     int err;
     char* errbuf;
     size_t errlen;
@@ -960,6 +962,20 @@ static double rng_sample(scen_t* s, int tidx, int idx) {
 }
 
 /* Incrementor::sample (src/proc/increment.rs:46-148) */
+/* Records one Poisson draw when the caller asked for a trace. */
+static uint64_t traced_poisson(scen_t* s, int tidx, int idx, double uu, double lam) {
+    uint64_t k = orc_poisson(uu, lam);
+    if (s->trace && s->trace_n < s->trace_max) {
+        orc_jump* r = &s->trace[s->trace_n++];
+        r->t = tidx;
+        r->idx = idx;
+        r->u = uu;
+        r->lam = lam;
+        r->k = k;
+    }
+    return k;
+}
+
 static double inc_sample(scen_t* s, const inc_t* inc, int tidx) {
     switch (inc->kind) {
     case INC_DT: return s->dts[tidx];
@@ -970,7 +986,7 @@ static double inc_sample(scen_t* s, const inc_t* inc, int tidx) {
     default: {
         double uu = rng_sample(s, tidx, inc->idx);
         double lam = feval(s, inc->lambda, s->times[tidx]) * s->dts[tidx];
-        return (double)orc_poisson(uu, lam);
+        return (double)traced_poisson(s, tidx, inc->idx, uu, lam);
     }
     }
 }
@@ -1075,7 +1091,7 @@ static double inc_sample_tb(scen_t* s, const inc_t* inc, int t, const double* ro
     double uu = rng_sample(s, t, inc->idx);
     fill_slots(s, s->times[t], row);
     double lam = ev(inc->lambda, s->slots) * s->dts[t];
-    return (double)orc_poisson(uu, lam);
+    return (double)traced_poisson(s, t, inc->idx, uu, lam);
 }
 
 static void euler_step_tb(scen_t* s, int t) {
@@ -1154,6 +1170,8 @@ typedef struct {
     uint64_t out_base;
     const enode* payoff;
     double sum, sumc, sq, sqc;
+    orc_jump* trace;
+    int trace_max, trace_n;
     int err;
     char errbuf[256];
 } job_t;
@@ -1180,6 +1198,9 @@ static void* run_job(void* arg) {
     s.nslots = 1 + P + u->n_params;
     s.errbuf = J->errbuf;
     s.errlen = sizeof J->errbuf;
+    s.trace = J->trace;
+    s.trace_max = J->trace_max;
+    s.trace_n = 0;
     s.times_strict = 1;
     for (int i = 1; i < T; ++i)
         if (!(J->times[i] > J->times[i - 1])) s.times_strict = 0;
@@ -1269,6 +1290,7 @@ static void* run_job(void* arg) {
         }
     }
     J->err = s.err;
+    J->trace_n = s.trace_n;
     free(s.dts); free(s.sqrt_dts); free(s.raw); free(s.slots); free(s.step_vals);
     free(s.sobol_vals); free(incs); free(va); free(vb); free(vc); free(prow); free(masks);
     return NULL;
@@ -1350,5 +1372,28 @@ int orc_eval_payoff(const orc_universe* u, const char* expr, double t, const dou
     }
     free(slots);
     enode_free(e);
+    return 0;
+}
+
+/* Every Poisson draw of one scenario (its step, stochastic index, uniform,
+ * lambda * dt and count), in draw order: the record that tells whether a
+ * jump count differing from another implementation's sits on a CDF
+ * boundary.  Test infrastructure only. */
+int orc_jump_trace(const orc_universe* u, const double* times, int n_times, const double* x0,
+                   uint64_t scenario, const orc_cfg* cfg, orc_jump* out, int max_out, int* n_out,
+                   char* err, size_t errlen) {
+    if (n_times < 1) { set_err(err, errlen, "need at least one time point"); return 2; }
+    if (cfg->scheme == ORC_RK && u->n_inc == 0 && n_times > 1) {
+        set_err(err, errlen, "RNG Index 0 out of bounds (max 0)");
+        return 6;
+    }
+    job_t J;
+    memset(&J, 0, sizeof J);
+    J.u = u; J.times = times; J.T = n_times; J.x0 = x0; J.cfg = cfg;
+    J.begin = scenario; J.end = scenario + 1; J.out_base = scenario;
+    J.trace = out; J.trace_max = max_out;
+    run_job(&J);
+    if (J.err) { set_err(err, errlen, "%s", J.errbuf); return 6; }
+    *n_out = J.trace_n;
     return 0;
 }

@@ -57,6 +57,14 @@ typedef struct orc_cfg {
     int icdf;       /* 0: AS 26.2.23 (reference); 1: the accurate option      */
 } orc_cfg;
 
+/* One Poisson draw (fast_inverse_poisson_cdf, src/proc/increment.rs:182-200):
+ * step t, stochastic index idx, uniform u, lambda * dt, count k. */
+typedef struct orc_jump {
+    int32_t t, idx;
+    double u, lam;
+    uint64_t k;
+} orc_jump;
+
 /* ---- universe (equation parsing, src/proc/util.rs:52-166) ------------- */
 int  orc_parse(const char* const* eqs, int n_eq,
                const char* const* param_names, const double* param_vals,
@@ -111,6 +119,11 @@ void orc_sobol_points(const uint32_t* V, int dims, uint64_t first, uint64_t n,
 double   orc_icdf_as26(double p);
 double   orc_icdf_accurate(double p);
 uint64_t orc_poisson(double u, double lambda);
+
+/* Every Poisson draw of scenario `scenario` in draw order (at most max_out). */
+int orc_jump_trace(const orc_universe* u, const double* times, int n_times, const double* x0,
+                   uint64_t scenario, const orc_cfg* cfg, orc_jump* out, int max_out, int* n_out,
+                   char* err, size_t errlen);
 
 #ifdef __cplusplus
 }

@@ -1331,18 +1331,38 @@ struct Gen {
         return u.token_kind[k] == IncKind::Dw ? V("w", k) : V("n", k);
     }
 
+    // One step's increments at local slot s of the segment buffers (LI, and
+    // LS for Runge-Kutta's sign) as named values.
+    void adj_load_incs(Out& o, bool rk) const {
+        for (int k = 0; k < NI; ++k) o.l("const " + R + " " + inc_store_name(k) + " = LI[s * " + S(NI) + " + " + S(k) + "];");
+        if (rk) o.l("const " + R + " sk = LS[s];");
+    }
+
+    // Adjoint of one coefficient evaluation c(Zset, tvar) weighted by the
+    // adjoint `w` of its value: the process adjoints `lset<q>` and the
+    // parameter gradients GP<m> take w * dc/dX_q and w * dc/dtheta_m.
+    void adj_coef(Out& o, const ExprP& c, const std::string& w, const std::string& zset, const std::string& tvar,
+                  const std::string& lset) const {
+        const int GP = (int)sp.grad_params.size();
+        for (int q = 0; q < P; ++q)
+            if (depends_on(c, VarKind::Process, q))
+                o.l("  " + lset + S(q) + " += " + w + " * " + ex(derivative(c, VarKind::Process, q), zset, tvar) + ";");
+        for (int m = 0; m < GP; ++m)
+            if (depends_on(c, VarKind::Param, sp.grad_params[m]))
+                o.l("  GP" + S(m) + " += " + w + " * " + ex(derivative(c, VarKind::Param, sp.grad_params[m]), zset, tvar) +
+                    ";");
+    }
+
+    // Steps between checkpoints of the batched adjoint: E = ceil(sqrt(n)) at
+    // run time, at most this many, so an instance takes at most
+    // kBatchAdjMaxSteps = 64 * 64 steps and its checkpoints and one segment's
+    // states and increments fit fixed per-thread arrays.
+    static constexpr int kBatchAdjE = 64;
+
     std::string adjoint(const std::string& name) {
-        // Pathwise adjoint of Euler-Maruyama: X' = X + sum_j c_j(t, X, theta) inc_j,
-        // lambda_t = lambda_{t+1} + sum_p lambda_{t+1,p} sum_j dc_pj/dX inc_j,
-        // g_theta += sum_p lambda_{t+1,p} sum_j dc_pj/dtheta inc_j.  Increments
-        // are held fixed (common random numbers); jump counts are piecewise
-        // constant in the parameters.
         mode = Mode::Forward;
         lane(0);
-        const int E = sp.ckpt_every;
-        const int K = (int)sp.payoffs.size();
-        const int GP = (int)sp.grad_params.size(), GX = (int)sp.grad_x0.size();
-        const int KT = K + GP + GX;
+        const int KT = (int)(sp.payoffs.size() + sp.grad_params.size() + sp.grad_x0.size());
         Out o;
         o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
         o.ind++;
@@ -1354,125 +1374,325 @@ struct Gen {
         for (int k = 0; k < (int)u.params.size(); ++k)
             o.l("const " + R + " PR" + S(k) + " = (" + R + ")__ldg(&a.params[" + S(k) + "]);");
         if (xorm()) o.l("const sde_u32* mask_rep = a.masks ? a.masks + (sde_u64)rep * a.mask_stride : nullptr;");
-        lane_prologue(o);
-        if (uses_chacha()) o.l("sde_u64 cblk = ~0ull; sde_u32 CB[16];");
-        o.l(R + "* CK = (" + R + "*)a.ckpt;");
-        o.l("const sde_u64 ckrow = (sde_u64)rep * a.n_ckpt;");
-        // the forward pass's increments, [rep][t][k][path], when the run
-        // holds a buffer for them: the reverse sweep then reads them instead
-        // of drawing them again
-        o.l(R + "* INC = (" + R + "*)a.inc;");
-        auto inc_at = [&](int k) {
-            return "INC[(((sde_u64)rep * n_steps + t) * " + S(NI) + "ull + " + S(k) + "ull) * a.n_paths + i]";
-        };
-        // forward pass with checkpoints
-        o.l("for (int t = 0; t < n_steps; ++t) {");
-        o.ind++;
-        o.l("if (t % " + S(E) + " == 0 && active) {");
-        for (int p = 0; p < P; ++p)
-            o.l("  CK[((ckrow + t / " + S(E) + ") * " + S(P) + " + " + S(p) + ") * a.n_paths + i] = X" + S(p) + ";");
-        o.l("}");
-        step_header(o);
-        uniforms_ra(o);
-        wiener(o);
-        step_reference(o);
-        if (NI > 0) {
-            o.l("if (INC && active) {");
-            for (int k = 0; k < NI; ++k) o.l("  " + inc_at(k) + " = " + inc_store_name(k) + ";");
-            o.l("}");
-        }
-        o.ind--;
-        o.l("}");
-        // payoffs and the terminal adjoint of payoff 0
-        o.l("const " + R + " tT = (" + R + ")__ldg(&a.times[a.T - 1]);");
         o.l("double fs[" + S(KT) + "] = {}, fq[" + S(KT) + "] = {};");
-        for (int k = 0; k < K; ++k)
-            o.l("fs[" + S(k) + "] = active ? (double)(" + ex(sp.payoffs[k], "X", "tT") + ") : 0.0;");
-        for (int p = 0; p < P; ++p)
-            o.l(R + " LA" + S(p) + " = " + ex(derivative(sp.payoffs[0], VarKind::Process, p), "X", "tT") + ";");
-        for (int m = 0; m < GP; ++m)
-            o.l(R + " GP" + S(m) + " = " + ex(derivative(sp.payoffs[0], VarKind::Param, sp.grad_params[m]), "X", "tT") + ";");
-        // reverse sweep over segments, recomputing each from its checkpoint
-        o.l(R + " LX[" + S(E * std::max(1, P)) + "];");
-        o.l(R + " LI[" + S(E * std::max(1, NI)) + "];");
-        o.l("const int nseg = (n_steps + " + S(E - 1) + ") / " + S(E) + ";");
-        o.l("for (int seg = nseg - 1; seg >= 0; --seg) {");
-        o.ind++;
-        o.l("const int s0 = seg * " + S(E) + ";");
-        o.l("const int s1 = min(s0 + " + S(E) + ", n_steps);");
-        for (int p = 0; p < P; ++p)
-            o.l("X" + S(p) + " = active ? CK[((ckrow + seg) * " + S(P) + " + " + S(p) + ") * a.n_paths + i] : X" + S(p) + ";");
-        o.l("for (int t = s0; t < s1; ++t) {");
-        o.ind++;
-        o.l("const int s = t - s0;");
-        for (int p = 0; p < P; ++p) o.l("LX[s * " + S(P) + " + " + S(p) + "] = X" + S(p) + ";");
-        step_header(o);
-        // the step's increments: stored by the forward pass, or drawn again
-        // (jump counts need the cache = X)
-        for (int p : u.levy) o.l("C" + S(p) + " = X" + S(p) + ";");
-        if (NI > 0) {
-            o.l(R + " IV[" + S(NI) + "];");
-            o.l("if (INC) {");
-            // (issuing a whole segment's loads ahead into LI was measured:
-            // slower, 2.23 against 2.08 ms for the GBM adjoint)
-            for (int k = 0; k < NI; ++k) o.l("  IV[" + S(k) + "] = active ? " + inc_at(k) + " : " + L(0.0) + ";");
-            o.l("} else {");
-            o.ind++;
-            uniforms_ra(o);
-            wiener(o);
-            poisson(o, "C", "tc");
-            for (int k = 0; k < NI; ++k) o.l("IV[" + S(k) + "] = " + inc_store_name(k) + ";");
-            o.ind--;
-            o.l("}");
-            for (int k = 0; k < NI; ++k) o.l("const " + R + " " + inc_store_name(k) + " = IV[" + S(k) + "];");
-        }
-        for (int k = 0; k < NI; ++k) o.l("LI[s * " + S(NI) + " + " + S(k) + "] = " + inc_store_name(k) + ";");
-        for (int p : u.levy) {
-            o.l(R + " N" + S(p) + " = X" + S(p) + ";");
-            for (const auto& tm : u.procs[p].terms)
-                o.l("N" + S(p) + " = N" + S(p) + " + " + ex(tm.coef, "C", "tc") + " * " + inc(tm) + ";");
-        }
-        for (int p : u.levy) o.l("X" + S(p) + " = N" + S(p) + ";");
-        o.ind--;
-        o.l("}");
-        o.l("for (int t = s1 - 1; t >= s0; --t) {");
-        o.ind++;
-        o.l("const int s = t - s0;");
-        o.l("const " + R + " tc = " + T("times") + ";");
-        o.l("const " + R + " dt = " + T("dts") + ";");
-        o.l("(void)tc; (void)dt;");
-        for (int p = 0; p < P; ++p) o.l("const " + R + " Y" + S(p) + " = LX[s * " + S(P) + " + " + S(p) + "];");
-        for (int k = 0; k < NI; ++k) o.l("const " + R + " " + inc_store_name(k) + " = LI[s * " + S(NI) + " + " + S(k) + "];");
-        for (int q = 0; q < P; ++q) o.l(R + " LN" + S(q) + " = " + L(0.0) + ";");
-        for (int p : u.levy) {
-            const auto& terms = u.procs[p].terms;
-            for (size_t j = 0; j < terms.size(); ++j) {
-                const ExprP& c = terms[j].coef;
-                const std::string li = "li" + S(p) + "_" + S((int)j);
-                o.l("{ const " + R + " " + li + " = LA" + S(p) + " * " + inc(terms[j]) + ";");
-                for (int q = 0; q < P; ++q)
-                    if (depends_on(c, VarKind::Process, q))
-                        o.l("  LN" + S(q) + " += " + li + " * " + ex(derivative(c, VarKind::Process, q), "Y", "tc") + ";");
-                for (int m = 0; m < GP; ++m)
-                    if (depends_on(c, VarKind::Param, sp.grad_params[m]))
-                        o.l("  GP" + S(m) + " += " + li + " * " +
-                            ex(derivative(c, VarKind::Param, sp.grad_params[m]), "Y", "tc") + ";");
-                o.l("}");
-            }
-        }
-        for (int q = 0; q < P; ++q) o.l("LA" + S(q) + " += LN" + S(q) + ";");
-        o.ind--;
-        o.l("}");
-        o.ind--;
-        o.l("}");
-        for (int m = 0; m < GP; ++m) o.l("fs[" + S(K + m) + "] = active ? (double)GP" + S(m) + " : 0.0;");
-        for (int x = 0; x < GX; ++x) o.l("fs[" + S(K + GP + x) + "] = active ? (double)LA" + S(sp.grad_x0[x]) + " : 0.0;");
+        adjoint_path(o, "fs");
         o.l("for (int k = 0; k < " + S(KT) + "; ++k) fq[k] = fs[k] * fs[k];");
         o.l("sde_block_reduce_store<" + S(KT) + ">(fs, fq, a.partials + (((sde_u64)rep * gridDim.x + blockIdx.x) * " +
             S(KT) + "u) * 4u);");
         o.ind--;
         o.l("}");
         return o.s.str();
+    }
+
+    // Device function of an adjoint template for the batched kernel: the
+    // thread's PPT paths one after another (each path's forward pass and
+    // reverse sweep), adding payoffs and gradients to fs / fq.  Uniform
+    // steps of the instance; checkpoints every ceil(sqrt(steps)) steps in
+    // per-thread arrays; increments drawn again in the reverse sweep.
+    std::string batch_adjoint_template(const std::string& name, int K, int ppt_lanes) {
+        mode = Mode::Batch;
+        lane(0);
+        const int KT = (int)(sp.payoffs.size() + sp.grad_params.size() + sp.grad_x0.size());
+        Out o;
+        o.l("static __device__ __forceinline__ void " + name +
+            "(const sde_batch_inst& in, sde_u64 first0, const sde_batch_args& a, double (&fs)[" + S(K) +
+            "], double (&fq)[" + S(K) + "]) {");
+        o.ind++;
+        shared_prologue(o);
+        o.l("int E = 1;");
+        o.l("while (E * E < n_steps) ++E;");
+        o.l("for (int lj = 0; lj < " + S(ppt_lanes) + "; ++lj) {");
+        o.ind++;
+        o.l("const sde_u64 first = first0 + (sde_u64)lj * blockDim.x;");
+        o.l("double pv[" + S(KT) + "] = {};");
+        adjoint_path(o, "pv");
+        o.l("for (int k = 0; k < " + S(KT) + "; ++k) { fs[k] += pv[k]; fq[k] += pv[k] * pv[k]; }");
+        o.ind--;
+        o.l("}");
+        o.ind--;
+        o.l("}");
+        mode = Mode::Forward;
+        return o.s.str();
+    }
+
+    // The step's time values in the reverse sweep.
+    void adj_step_times(Out& o, bool rk) const {
+        if (mode == Mode::Forward) {
+            o.l("const " + R + " tc = " + T("times") + ";");
+            o.l("const " + R + " dt = " + T("dts") + ";");
+            if (rk) {
+                o.l("const " + R + " tn = " + T("times", "t + 1") + ";");
+                o.l("const " + R + " sdt = " + T("sqrt_dts") + ";");
+            }
+        } else {
+            o.l("const " + R + " tc = (" + R + ")t * bdt;");
+            o.l("const " + R + " dt = bdt;");
+            if (rk) {
+                o.l("const " + R + " tn = (" + R + ")(t + 1) * bdt;");
+                o.l("const " + R + " sdt = bsdt;");
+            }
+        }
+        o.l("(void)tc; (void)dt;");
+        if (rk) o.l("(void)tn; (void)sdt;");
+    }
+
+    // One path's forward pass with checkpoints and reverse sweep; writes the
+    // path's payoffs and gradients into out[] (zeros for an inactive lane).
+    //
+    // Pathwise adjoint of the step recursion, increments held fixed
+    // (common random numbers; jump counts are piecewise constant in the
+    // parameters).
+    //
+    // Euler-Maruyama: X' = X + sum_j c_j(t, X, theta) inc_j, so
+    //   lambda_t = lambda_{t+1} + sum_p lambda_{t+1,p} sum_j dc_pj/dX inc_j,
+    //   g_theta += sum_p lambda_{t+1,p} sum_j dc_pj/dtheta inc_j.
+    //
+    // Runge-Kutta (src/sim/runge_kutta.rs:17-97), sign sk = +-1 from the
+    // step's uniform 0 held fixed:
+    //   a_pj = c_pj(Z, t)          k1_p = sum_j a_pj inc_j
+    //   pe_p = sum_{j in dW} a_pj sk sqrt(dt)
+    //   B_p  = X_p + k1_p + pe_p   (the probe)
+    //   k2_p = sum_j c_pj(B, t + dt) inc_j
+    //   X'_p = X_p + (k1_p + k2_p) / 2
+    // Z is the state the stage-1 coefficients see: X itself in textbook
+    // semantics; in the reference's semantics the name->value cache, which
+    // a step leaves at its probe B and the next step's stage 1 reads without
+    // a refresh (src/func.rs:32-42: eval at an unchanged time keeps the
+    // cache).  The cache is then part of the state: C' = B, C_0 = X_0,
+    // checkpointed beside X, with its own adjoint LC.  Reverse:
+    //   lB  = LC (reference semantics, else 0) + sum_pj (LA_p / 2) inc_j dc_pj/dB
+    //   lk1 = LA / 2 + lB,  lpe = lB
+    //   lZ  = sum_pj (lk1_p inc_j + [dW] lpe_p sk sqrt(dt)) dc_pj/dZ
+    //   LA <- LA + lB (+ lZ in textbook semantics),  LC <- lZ.
+    void adjoint_path(Out& o, const std::string& out) {
+        const bool batch = mode == Mode::Batch;
+        const bool rk = sp.scheme == SCHEME_RK;
+        const bool refc = rk && sp.semantics == SEM_REFERENCE;
+        const int PS = refc ? 2 * P : P;          // checkpointed values per path
+        const int NS = rk ? NI + 1 : NI;          // stored values per step (+ RK's sign)
+        const std::string E = batch ? "E" : S(sp.ckpt_every);
+        const int EMAX = batch ? kBatchAdjE : sp.ckpt_every;
+        const int K = (int)sp.payoffs.size();
+        const int GP = (int)sp.grad_params.size(), GX = (int)sp.grad_x0.size();
+        const std::string Zs = refc ? "Z" : "Y";  // stage-1 evaluation point in the reverse sweep
+        o.l("{");
+        o.ind++;
+        lane_prologue(o);
+        if (uses_chacha()) o.l("sde_u64 cblk = ~0ull; sde_u32 CB[16];");
+        // checkpoints: [rep][n_ckpt][PS][path] in device memory for the plan
+        // kernel; a per-thread array for the batched template
+        std::function<std::string(const std::string&, int)> ck_at;
+        if (batch) {
+            o.l(R + " CKL[" + S(kBatchAdjE * PS) + "];");
+            ck_at = [&](const std::string& seg, int v) { return "CKL[(" + seg + ") * " + S(PS) + " + " + S(v) + "]"; };
+        } else {
+            o.l(R + "* CK = (" + R + "*)a.ckpt;");
+            o.l("const sde_u64 ckrow = (sde_u64)rep * a.n_ckpt;");
+            ck_at = [&](const std::string& seg, int v) {
+                return "CK[((ckrow + " + seg + ") * " + S(PS) + " + " + S(v) + ") * a.n_paths + i]";
+            };
+            // the forward pass's increments (and RK's sign),
+            // [rep][t][slot][path], when the run holds a buffer for them: the
+            // reverse sweep then reads them instead of drawing them again
+            o.l(R + "* INC = (" + R + "*)a.inc;");
+        }
+        auto inc_at = [&](int k) {
+            return "INC[(((sde_u64)rep * n_steps + t) * " + S(NS) + "ull + " + S(k) + "ull) * a.n_paths + i]";
+        };
+        // forward pass with checkpoints
+        o.l("for (int t = 0; t < n_steps; ++t) {");
+        o.ind++;
+        o.l("if (t % " + E + " == 0 && active) {");
+        for (int p = 0; p < P; ++p) o.l("  " + ck_at("t / " + E, p) + " = X" + S(p) + ";");
+        if (refc)
+            for (int p = 0; p < P; ++p) o.l("  " + ck_at("t / " + E, P + p) + " = C" + S(p) + ";");
+        o.l("}");
+        step_header(o);
+        uniforms_ra(o);
+        wiener(o);
+        if (rk) step(o);
+        else step_reference(o);
+        if (NS > 0 && !batch) {
+            o.l("if (INC && active) {");
+            for (int k = 0; k < NI; ++k) o.l("  " + inc_at(k) + " = " + inc_store_name(k) + ";");
+            if (rk) o.l("  " + inc_at(NI) + " = sk;");
+            o.l("}");
+        }
+        o.ind--;
+        o.l("}");
+        // payoffs and the terminal adjoint of payoff 0
+        o.l("const " + R + " tT = " + (batch ? "(" + R + ")n_steps * bdt" : "(" + R + ")__ldg(&a.times[a.T - 1])") + ";");
+        for (int k = 0; k < K; ++k)
+            o.l(out + "[" + S(k) + "] = active ? (double)(" + ex(sp.payoffs[k], "X", "tT") + ") : 0.0;");
+        for (int p = 0; p < P; ++p)
+            o.l(R + " LA" + S(p) + " = " + ex(derivative(sp.payoffs[0], VarKind::Process, p), "X", "tT") + ";");
+        if (refc)
+            for (int p = 0; p < P; ++p) o.l(R + " LC" + S(p) + " = " + L(0.0) + ";");
+        for (int m = 0; m < GP; ++m)
+            o.l(R + " GP" + S(m) + " = " + ex(derivative(sp.payoffs[0], VarKind::Param, sp.grad_params[m]), "X", "tT") + ";");
+        // reverse sweep over segments, recomputing each from its checkpoint
+        o.l(R + " LX[" + S(EMAX * std::max(1, P)) + "];");
+        if (refc) o.l(R + " LZ[" + S(EMAX * std::max(1, P)) + "];");
+        o.l(R + " LI[" + S(EMAX * std::max(1, NI)) + "];");
+        if (rk) o.l(R + " LS[" + S(EMAX) + "];");
+        o.l("const int nseg = (n_steps + " + E + " - 1) / " + E + ";");
+        o.l("for (int seg = nseg - 1; seg >= 0; --seg) {");
+        o.ind++;
+        o.l("const int s0 = seg * " + E + ";");
+        o.l("const int s1 = min(s0 + " + E + ", n_steps);");
+        for (int p = 0; p < P; ++p) o.l("X" + S(p) + " = active ? " + ck_at("seg", p) + " : X" + S(p) + ";");
+        if (refc)
+            for (int p = 0; p < P; ++p) o.l("C" + S(p) + " = active ? " + ck_at("seg", P + p) + " : C" + S(p) + ";");
+        o.l("for (int t = s0; t < s1; ++t) {");
+        o.ind++;
+        o.l("const int s = t - s0;");
+        for (int p = 0; p < P; ++p) o.l("LX[s * " + S(P) + " + " + S(p) + "] = X" + S(p) + ";");
+        if (refc)
+            for (int p = 0; p < P; ++p) o.l("LZ[s * " + S(P) + " + " + S(p) + "] = C" + S(p) + ";");
+        step_header(o);
+        // the step's increments: stored by the forward pass, or drawn again
+        // (jump counts read the cache: the state itself but in reference RK)
+        if (!refc)
+            for (int p : u.levy) o.l("C" + S(p) + " = X" + S(p) + ";");
+        if (NS > 0) {
+            o.l(R + " IV[" + S(NS) + "];");
+            if (!batch) {
+                o.l("if (INC) {");
+                // (issuing a whole segment's loads ahead into LI was measured:
+                // slower, 2.23 against 2.08 ms for the GBM adjoint)
+                for (int k = 0; k < NS; ++k) o.l("  IV[" + S(k) + "] = active ? " + inc_at(k) + " : " + L(0.0) + ";");
+                o.l("} else {");
+            } else {
+                o.l("{");
+            }
+            o.ind++;
+            uniforms_ra(o);
+            wiener(o);
+            poisson(o, "C", "tc");
+            for (int k = 0; k < NI; ++k) o.l("IV[" + S(k) + "] = " + inc_store_name(k) + ";");
+            if (rk) o.l("IV[" + S(NI) + "] = " + sk_expr() + ";");
+            o.ind--;
+            o.l("}");
+            for (int k = 0; k < NI; ++k) o.l("const " + R + " " + inc_store_name(k) + " = IV[" + S(k) + "];");
+            if (rk) o.l("const " + R + " sk = IV[" + S(NI) + "];");
+        }
+        for (int k = 0; k < NI; ++k) o.l("LI[s * " + S(NI) + " + " + S(k) + "] = " + inc_store_name(k) + ";");
+        if (rk) {
+            o.l("LS[s] = sk;");
+            // stage 1 at the cache (reference) or the state (textbook), the
+            // probe, stage 2 at the probe: the forward step, term by term
+            const std::string zc = refc ? "C" : "X";
+            for (int p : u.levy) {
+                const auto& terms = u.procs[p].terms;
+                o.l(R + " k1_" + S(p) + " = " + L(0.0) + ", pe" + S(p) + " = " + L(0.0) + ";");
+                for (size_t j = 0; j < terms.size(); ++j) {
+                    const std::string a = "a" + S(p) + "_" + S((int)j);
+                    o.l("{ const " + R + " " + a + " = " + ex(terms[j].coef, zc, "tc") + ";");
+                    o.l("  k1_" + S(p) + " = k1_" + S(p) + " + " + a + " * " + inc(terms[j]) + ";");
+                    if (terms[j].kind == IncKind::Dw) o.l("  pe" + S(p) + " = pe" + S(p) + " + " + a + " * sk * sdt;");
+                    o.l("}");
+                }
+            }
+            for (int p : u.levy) o.l("const " + R + " B" + S(p) + " = X" + S(p) + " + k1_" + S(p) + " + pe" + S(p) + ";");
+            for (int p : u.levy) {
+                const auto& terms = u.procs[p].terms;
+                o.l(R + " k2_" + S(p) + " = " + L(0.0) + ";");
+                for (size_t j = 0; j < terms.size(); ++j)
+                    o.l("k2_" + S(p) + " = k2_" + S(p) + " + " + ex(terms[j].coef, "B", "tn") + " * " + inc(terms[j]) + ";");
+            }
+            for (int p : u.levy) o.l("X" + S(p) + " = X" + S(p) + " + " + L(0.5) + " * (k1_" + S(p) + " + k2_" + S(p) + ");");
+            if (refc)
+                for (int p : u.levy) o.l("C" + S(p) + " = B" + S(p) + ";");
+        } else {
+            for (int p : u.levy) {
+                o.l(R + " N" + S(p) + " = X" + S(p) + ";");
+                for (const auto& tm : u.procs[p].terms)
+                    o.l("N" + S(p) + " = N" + S(p) + " + " + ex(tm.coef, "C", "tc") + " * " + inc(tm) + ";");
+            }
+            for (int p : u.levy) o.l("X" + S(p) + " = N" + S(p) + ";");
+        }
+        o.ind--;
+        o.l("}");
+        o.l("for (int t = s1 - 1; t >= s0; --t) {");
+        o.ind++;
+        o.l("const int s = t - s0;");
+        adj_step_times(o, rk);
+        for (int p = 0; p < P; ++p) o.l("const " + R + " Y" + S(p) + " = LX[s * " + S(P) + " + " + S(p) + "];");
+        adj_load_incs(o, rk);
+        if (!rk) {
+            for (int q = 0; q < P; ++q) o.l(R + " LN" + S(q) + " = " + L(0.0) + ";");
+            for (int p : u.levy) {
+                const auto& terms = u.procs[p].terms;
+                for (size_t j = 0; j < terms.size(); ++j) {
+                    const std::string li = "li" + S(p) + "_" + S((int)j);
+                    o.l("{ const " + R + " " + li + " = LA" + S(p) + " * " + inc(terms[j]) + ";");
+                    adj_coef(o, terms[j].coef, li, "Y", "tc", "LN");
+                    o.l("}");
+                }
+            }
+            for (int q = 0; q < P; ++q) o.l("LA" + S(q) + " += LN" + S(q) + ";");
+        } else {
+            if (refc)
+                for (int p = 0; p < P; ++p) o.l("const " + R + " Z" + S(p) + " = LZ[s * " + S(P) + " + " + S(p) + "];");
+            // the probe again, from the stage-1 coefficients
+            for (int p = 0; p < P; ++p) {
+                if (!u.procs[p].levy) {
+                    o.l("const " + R + " B" + S(p) + " = Y" + S(p) + ";");
+                    continue;
+                }
+                const auto& terms = u.procs[p].terms;
+                o.l(R + " k1_" + S(p) + " = " + L(0.0) + ", pe" + S(p) + " = " + L(0.0) + ";");
+                for (size_t j = 0; j < terms.size(); ++j) {
+                    const std::string a = "a" + S(p) + "_" + S((int)j);
+                    o.l("{ const " + R + " " + a + " = " + ex(terms[j].coef, Zs, "tc") + ";");
+                    o.l("  k1_" + S(p) + " = k1_" + S(p) + " + " + a + " * " + inc(terms[j]) + ";");
+                    if (terms[j].kind == IncKind::Dw) o.l("  pe" + S(p) + " = pe" + S(p) + " + " + a + " * sk * sdt;");
+                    o.l("}");
+                }
+                o.l("const " + R + " B" + S(p) + " = Y" + S(p) + " + k1_" + S(p) + " + pe" + S(p) + ";");
+            }
+            // stage 2: k2_p = sum_j c_pj(B, tn) inc_j, weighted by LA_p / 2
+            for (int q = 0; q < P; ++q) o.l(R + " lB" + S(q) + " = " + (refc ? "LC" + S(q) : L(0.0)) + ";");
+            for (int p : u.levy) {
+                const auto& terms = u.procs[p].terms;
+                for (size_t j = 0; j < terms.size(); ++j) {
+                    const std::string w = "w2_" + S(p) + "_" + S((int)j);
+                    o.l("{ const " + R + " " + w + " = " + L(0.5) + " * LA" + S(p) + " * " + inc(terms[j]) + ";");
+                    adj_coef(o, terms[j].coef, w, "B", "tn", "lB");
+                    o.l("}");
+                }
+            }
+            // stage 1: a_pj = c_pj(Z, tc) feeds k1 and the perturbation
+            for (int q = 0; q < P; ++q) o.l(R + " lZ" + S(q) + " = " + L(0.0) + ";");
+            for (int p : u.levy) {
+                const auto& terms = u.procs[p].terms;
+                o.l("const " + R + " lk1_" + S(p) + " = " + L(0.5) + " * LA" + S(p) + " + lB" + S(p) + ";");
+                for (size_t j = 0; j < terms.size(); ++j) {
+                    const std::string w = "w1_" + S(p) + "_" + S((int)j);
+                    std::string wv = "lk1_" + S(p) + " * " + inc(terms[j]);
+                    if (terms[j].kind == IncKind::Dw) wv += " + lB" + S(p) + " * sk * sdt";
+                    o.l("{ const " + R + " " + w + " = " + wv + ";");
+                    adj_coef(o, terms[j].coef, w, Zs, "tc", "lZ");
+                    o.l("}");
+                }
+            }
+            for (int q = 0; q < P; ++q)
+                o.l("LA" + S(q) + " = LA" + S(q) + " + lB" + S(q) + (refc ? "" : " + lZ" + S(q)) + ";");
+            if (refc)
+                for (int q = 0; q < P; ++q) o.l("LC" + S(q) + " = lZ" + S(q) + ";");
+        }
+        o.ind--;
+        o.l("}");
+        o.ind--;
+        o.l("}");
+        for (int m = 0; m < GP; ++m) o.l(out + "[" + S(K + m) + "] = active ? (double)GP" + S(m) + " : 0.0;");
+        // X0 feeds the state and, in reference RK, the cache C_0 = X_0
+        for (int x = 0; x < GX; ++x) {
+            const std::string q = S(sp.grad_x0[x]);
+            o.l(out + "[" + S(K + GP + x) + "] = active ? (double)(LA" + q + (refc ? " + LC" + q : "") + ") : 0.0;");
+        }
+        o.ind--;
+        o.l("}");
     }
 };
 
@@ -1615,10 +1835,11 @@ std::string generate_batch_source(const std::vector<const Universe*>& us, const 
     for (int ppt : ppts)
         for (size_t t = 0; t < us.size(); ++t) {
             KernelSpec s = specs[t];
-            s.ppt = ppt;
+            s.ppt = s.adjoint ? 1 : ppt;
             s.store_output = false;
             Gen g(*us[t], s);
-            src += g.batch_template("sde_tmpl" + std::to_string(t) + "_p" + std::to_string(ppt), K) + "\n";
+            const std::string nm = "sde_tmpl" + std::to_string(t) + "_p" + std::to_string(ppt);
+            src += (s.adjoint ? g.batch_adjoint_template(nm, K, ppt) : g.batch_template(nm, K)) + "\n";
         }
     for (const auto& v : variants) {
         const int block = v.first, ppt = v.second;

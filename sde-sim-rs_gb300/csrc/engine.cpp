@@ -450,7 +450,6 @@ static sde_plan* plan_create(const std::vector<std::string>& eqs, const std::vec
     for (const auto& s : payoffs) p->spec.payoffs.push_back(p->u.resolve(parse_expression(s)));
     if (grad_params || grad_x0) {
         if (p->spec.payoffs.empty()) fail(SDE_ERR_INVALID, "an adjoint plan needs a payoff");
-        if (p->spec.scheme != SCHEME_EULER) fail(SDE_ERR_UNSUPPORTED, "the adjoint is built for Euler-Maruyama");
         if (!p->u.alg.empty()) fail(SDE_ERR_UNSUPPORTED, "the adjoint does not take algebraic processes");
         p->spec.adjoint = true;
         for (const auto& g : *grad_params) {
@@ -679,16 +678,22 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
     }
 
     if (p->spec.adjoint) {
-        // checkpoints [rep][n_ckpt][P][path]: the state at every ckpt_every-th step
+        // checkpoints [rep][n_ckpt][PS][path]: the state at every
+        // ckpt_every-th step; Runge-Kutta in the reference's semantics also
+        // carries the name->value cache that the next step's stage 1 reads
+        // (PS = 2P), the other schemes the P processes
+        const bool rk = p->spec.scheme == SCHEME_RK;
+        const int PS = (rk && p->spec.semantics == SEM_REFERENCE ? 2 : 1) * std::max(1, P);
         const int E = p->spec.ckpt_every;
         A.ckpt_every = E;
         A.n_ckpt = std::max(1, (T - 1 + E - 1) / E);
-        r->ckpt = DBuf((size_t)A.n_ckpt * std::max(1, P) * N * a.n_replicates * r->elem + 8);
+        r->ckpt = DBuf((size_t)A.n_ckpt * PS * N * a.n_replicates * r->elem + 8);
         A.ckpt = r->ckpt.as<float>();
-        // the forward pass's increments [rep][T-1][NI][path], kept for the
-        // reverse sweep when they fit in a quarter of the free memory (the
-        // sweep otherwise draws them again: ChaCha blocks and normals)
-        const size_t inc_bytes = (size_t)(T - 1) * NI * N * a.n_replicates * r->elem;
+        // the forward pass's increments (and Runge-Kutta's sign)
+        // [rep][T-1][NI (+1)][path], kept for the reverse sweep when they fit
+        // in a quarter of the free memory (the sweep otherwise draws them
+        // again: ChaCha blocks and normals)
+        const size_t inc_bytes = (size_t)(T - 1) * (NI + (rk && NI > 0 ? 1 : 0)) * N * a.n_replicates * r->elem;
         size_t free_b = 0, total_b = 0;
         if (!p->adjoint_recompute && inc_bytes > 0 && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
             inc_bytes <= free_b / 4) {
@@ -1273,6 +1278,10 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 
 namespace sde {
 
+// The batched adjoint template checkpoints every ceil(sqrt(steps)) steps in
+// per-thread arrays of 64 checkpoints and 64 steps.
+constexpr int kBatchAdjointMaxSteps = 64 * 64;
+
 // candidate (block, paths per thread) shapes the autotuner times
 static const std::vector<std::pair<int, int>> kBatchVariants = {
     {128, 1}, {256, 1}, {128, 2}, {256, 2}, {128, 4}};
@@ -1413,14 +1422,15 @@ int sde_batch_create(const sde_plan* const* templates, int32_t n_templates, sde_
             const sde_plan* p = templates[t];
             if (!p) fail(SDE_ERR_INVALID, "NULL template");
             if (p->spec.rng != RNG_PSEUDO) fail(SDE_ERR_UNSUPPORTED, "batched templates use the pseudo-random streams");
-            if (p->spec.adjoint) fail(SDE_ERR_UNSUPPORTED, "batched templates are forward plans");
             if (t > 0 && p->spec.precision != templates[0]->spec.precision)
                 fail(SDE_ERR_INVALID, "batched templates must share one precision");
             if (p->spec.scheme == SCHEME_RK && p->u.n_stochastic() == 0)
                 fail(SDE_ERR_RNG_INDEX, "RNG Index 0 out of bounds (max 0)");
             b->u.push_back(p->u);
             b->specs.push_back(p->spec);
-            b->K = std::max(b->K, (int)p->spec.payoffs.size());
+            // an adjoint template's estimates: its payoffs, then the
+            // gradients of payoff 0 (as its plan's runs return them)
+            b->K = std::max(b->K, (int)(p->spec.payoffs.size() + p->spec.grad_params.size() + p->spec.grad_x0.size()));
         }
         if (b->K < 1) fail(SDE_ERR_INVALID, "batched templates need at least one payoff");
         for (auto& u : b->u) us.push_back(&u);
@@ -1463,6 +1473,9 @@ int sde_batch_prepare(sde_batch* b, const sde_batch_instances* in, int32_t autot
             const int t = in->template_id[i];
             if (t < 0 || t >= (int)b->u.size()) fail(SDE_ERR_INVALID, "template_id out of range");
             if (in->n_steps[i] < 1) fail(SDE_ERR_INVALID, "n_steps must be >= 1");
+            if (b->specs[t].adjoint && in->n_steps[i] > kBatchAdjointMaxSteps)
+                fail(SDE_ERR_UNSUPPORTED, "a batched adjoint instance takes at most " +
+                                              std::to_string(kBatchAdjointMaxSteps) + " steps");
             if (!(in->t_end[i] > 0)) fail(SDE_ERR_INVALID, "t_end must be positive");
             if ((int)b->u[t].params.size() > in->param_stride)
                 fail(SDE_ERR_INVALID, "param_stride is smaller than a template's parameter count");

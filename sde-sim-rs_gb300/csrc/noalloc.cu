@@ -90,6 +90,7 @@ extern "C" int sde_run_estimates_static(sde_plan* plan, const double* times, int
                                         int32_t n_replicates, uint64_t seed, void* stream, double* host_sum,
                                         double* host_sumsq) {
     if (!plan || !times || !host_sum || !host_sumsq) return fail_with(SDE_ERR_INVALID, "NULL argument");
+    if ((n_x0 > 0 && !x0) || (n_params > 0 && !params)) return fail_with(SDE_ERR_INVALID, "NULL argument");
     const int T = n_times;
     if (T < 1) return fail_with(SDE_ERR_INVALID, "need at least one time point");
     for (int t = 1; t < T; ++t)
@@ -111,7 +112,8 @@ extern "C" int sde_run_estimates_static(sde_plan* plan, const double* times, int
         return fail_with(SDE_ERR_RNG_INDEX, "RNG Index 0 out of bounds (max 0)");
     const int P = v.n_processes, K = v.n_payoffs, Tm1 = T > 1 ? T - 1 : 1;
     const uint64_t per_block = (uint64_t)v.block * (uint64_t)v.ppt;
-    const uint64_t gx = (n_paths + per_block - 1) / per_block;
+    const uint64_t gx = n_paths / per_block + (n_paths % per_block != 0);
+    if (gx > 0x7fffffffull) return fail_with(SDE_ERR_INVALID, "too many paths for one launch");
     // scratch layout, every piece 256-byte aligned
     size_t off = 0;
     const size_t o_times = off; off = align256(off + (size_t)T * 8);
@@ -142,22 +144,29 @@ extern "C" int sde_run_estimates_static(sde_plan* plan, const double* times, int
         return SDE_OK;
     }
     cudaStream_t s = (cudaStream_t)stream;
+    // From the first copy on, a failure first waits for what this call has
+    // already queued on s, so no work of a failed call is left writing the
+    // shared array when the caller's next call starts.
+    auto async_fail = [s](cudaError_t err, const char* what) {
+        (void)cudaStreamSynchronize(s);
+        return cuda_fail(err, what);
+    };
     double* d_times = (double*)(base + o_times);
     double* d_x0 = (double*)(base + o_x0);
     double* d_par = (double*)(base + o_par);
     double* d_est = (double*)(base + o_est);
     if ((e = cudaMemcpyAsync(d_times, times, (size_t)T * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return cuda_fail(e, "stage times");
-    if ((e = cudaMemsetAsync(d_x0, 0, (size_t)(P > 0 ? P : 1) * 8, s)) != cudaSuccess) return cuda_fail(e, "stage x0");
+        return async_fail(e, "stage times");
+    if ((e = cudaMemsetAsync(d_x0, 0, (size_t)(P > 0 ? P : 1) * 8, s)) != cudaSuccess) return async_fail(e, "stage x0");
     if (n_x0 > 0 && (e = cudaMemcpyAsync(d_x0, x0, (size_t)n_x0 * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return cuda_fail(e, "stage x0");
+        return async_fail(e, "stage x0");
     if (n_params > 0 &&
         (e = cudaMemcpyAsync(d_par, params, (size_t)n_params * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return cuda_fail(e, "stage params");
+        return async_fail(e, "stage params");
     k_stage_time_grid<<<1, 256, 0, s>>>(d_times, T, (double*)(base + o_dts), (double*)(base + o_sdts),
                                         (float*)(base + o_tf), (float*)(base + o_dtf), (float*)(base + o_sdtf),
                                         (int*)(base + o_tidx));
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "stage time grid");
+    if ((e = cudaGetLastError()) != cudaSuccess) return async_fail(e, "stage time grid");
     sde_args A;
     std::memset(&A, 0, sizeof A);
     A.times = d_times;
@@ -177,16 +186,16 @@ extern "C" int sde_run_estimates_static(sde_plan* plan, const double* times, int
     void* kargs[] = {&A};
     if ((e = cudaLaunchKernel((const void*)v.kernel, dim3((unsigned)gx, (unsigned)n_replicates), dim3(v.block), kargs,
                               0, s)) != cudaSuccess)
-        return cuda_fail(e, "step kernel launch");
+        return async_fail(e, "step kernel launch");
     if ((e = launch_reduce_partials(A.partials, (int)gx, K, n_replicates, d_est, s)) != cudaSuccess)
-        return cuda_fail(e, "estimator reduction");
+        return async_fail(e, "estimator reduction");
     // [rep][K][2] -> the caller's [rep][K] sums and sums of squares
     if ((e = cudaMemcpy2DAsync(host_sum, 8, d_est, 16, 8, (size_t)n_replicates * K, cudaMemcpyDeviceToHost, s)) !=
         cudaSuccess)
-        return cuda_fail(e, "estimates D2H");
+        return async_fail(e, "estimates D2H");
     if ((e = cudaMemcpy2DAsync(host_sumsq, 8, d_est + 1, 16, 8, (size_t)n_replicates * K, cudaMemcpyDeviceToHost,
                                s)) != cudaSuccess)
-        return cuda_fail(e, "estimates D2H");
+        return async_fail(e, "estimates D2H");
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "kernel execution");
     return SDE_OK;
 }

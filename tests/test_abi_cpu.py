@@ -128,10 +128,17 @@ def test_adjoint_lowering_compiles(engine, precision, rng, scramble):
                     rng=rng, scramble=scramble, output="none")
     assert p.n_payoffs == 2 + 4 + 2
     assert "sde_adjoint_euler" in p.source
+    # Runge-Kutta in both semantics: the reference's carries the cache (the
+    # previous step's probe) as state, checkpointed beside the processes
+    for sem in ("reference", "textbook"):
+        q = engine.Plan(eqs, params=["kappa", "theta", "xi", "rho", "mu"], payoffs=["max(S - 100, 0)"],
+                        grad_params=["kappa", "rho"], grad_x0=["v"], precision=precision, rng=rng,
+                        scramble=scramble, output="none", scheme="runge-kutta", semantics=sem)
+        assert "sde_adjoint_rk" in q.source and ("LC0" in q.source) == (sem == "reference")
     # jump terms are held fixed in the reverse sweep; algebraic processes
-    # and Runge-Kutta are not differentiated
+    # are not differentiated
     engine.Plan(["dX = (mu * X) * dt + (0.1 * X) * dN1(2.0)"], params=["mu"], payoffs=["X"],
-                grad_params=["mu"], precision=precision)
+                grad_params=["mu"], precision=precision, scheme="runge-kutta")
     with pytest.raises(Exception, match="algebraic"):
         engine.Plan(["dX = (mu * X) * dt + (0.1) * dW1", "Y = X"], params=["mu"], payoffs=["X"],
                     grad_params=["mu"])
@@ -367,3 +374,21 @@ def test_register_budgets_of_the_measured_kernels(engine):
         spill, regs = seen[name]
         assert spill == 0, name
         assert regs <= cap, (name, regs, cap)
+
+
+def test_rust_shim_declarations_match_header():
+    """The extern block of the Rust shim declares each function with the
+    header's parameter count (sde-sim-rs_gb300/rust/src/gpu.rs, which has
+    no compiler here)."""
+    with open(os.path.join(ROOT, "sde-sim-rs_gb300", "rust", "src", "gpu.rs")) as f:
+        rs = f.read()
+    block = re.search(r'unsafe extern "C" \{(.*?)\n\}', rs, re.S).group(1)
+    rust = {m.group(1): [a for a in m.group(2).split(",") if a.strip()]
+            for m in re.finditer(r"fn (sde_\w+)\((.*?)\)\s*->", block, re.S)}
+    with open(os.path.join(ROOT, "include", "sdegpu.h")) as f:
+        hdr = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+    assert set(rust) == {"sde_simulate", "sde_result_shape", "sde_result_copy_long", "sde_result_destroy",
+                         "sde_last_error"}
+    for name, args in rust.items():
+        decl = re.search(r"\b" + name + r"\s*\((.*?)\);", hdr, re.S).group(1)
+        assert len(args) == len([a for a in decl.split(",") if a.strip()]), name

@@ -91,3 +91,87 @@ def test_batch_autotune_and_replay(engine):
     sd = x0[g, 0] * np.exp(params[g, 0]) * np.sqrt(np.exp(params[g, 1] ** 2) - 1)
     z = (m - exact) / (sd / np.sqrt(paths[g]))
     assert np.mean(np.abs(z) < 4) > 0.97
+
+
+# ---- batched forward + adjoint ------------------------------------------------
+# Adjoint plans as templates: every instance returns its payoffs and the
+# pathwise gradients of payoff 0, as the template's own runs do (one
+# universe per call in the reference, src/sim/mod.rs:20-92).  The batched
+# template checkpoints every ceil(sqrt(steps)) steps instead of the plan's
+# spacing, and its time grid is t * (t_end / steps): the gradients agree with
+# per-instance adjoint runs to rounding.
+
+HESTON_P = ["dv = (kappa * (theta - max(v, 0))) * dt + (xi * max(v, 0)^0.5) * dW1",
+            "dS = (mu * S) * dt + (rho * max(v, 0)^0.5 * S) * dW1 + "
+            "((1 - rho^2)^0.5 * max(v, 0)^0.5 * S) * dW2"]
+
+
+def _adjoint_templates(engine, precision):
+    tg = engine.Plan(GBM_T, params=["mu", "sigma"], payoffs=["max(X - 100, 0)", "X"], grad_params=["mu", "sigma"],
+                     grad_x0=["X"], precision=precision, output="none")
+    to = engine.Plan(OU_T, params=["theta", "m", "s"], payoffs=["X"], grad_params=["theta", "m", "s"],
+                     grad_x0=["X"], precision=precision, output="none")
+    th = engine.Plan(HESTON_P, params=["kappa", "theta", "xi", "rho", "mu"], payoffs=["max(S - 100, 0)"],
+                     grad_params=["kappa", "xi", "rho"], grad_x0=["v"], precision=precision, output="none",
+                     scheme="runge-kutta")
+    return [tg, to, th]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batched_adjoint_matches_per_instance_adjoint_runs(engine, precision):
+    from sde_sim_rs.batch import Batch
+    n = 30
+    tid, steps, paths, seeds, x0, params = make_instances(n, 23, max_steps=300, max_log2_paths=11)
+    tid[::3] = 2                                   # every third instance: Heston, Runge-Kutta
+    hx0 = np.tile([0.04, 100.0], (n, 1))
+    hpar = np.tile([2.0, 0.04, 0.3, -0.7, 0.03], (n, 1))
+    X0 = np.where((tid == 2)[:, None], hx0, np.pad(x0, ((0, 0), (0, 1))))
+    PAR = np.where((tid == 2)[:, None], hpar, np.pad(params, ((0, 0), (0, 2))))
+    templates = _adjoint_templates(engine, precision)
+    job = Batch(templates).prepare(tid, steps, 1.0, paths, seeds, X0, PAR)
+    s, q = job.run().results()
+    assert s.shape == (n, 6)   # GBM: 2 payoffs + 3 gradients; widest template
+    for i in range(n):
+        plan = templates[tid[i]]
+        times = np.arange(steps[i] + 1) / steps[i]
+        init = {nm: X0[i, plan.index(nm)] for nm in plan.process_names}
+        rs, rq = plan.run(times, init, int(paths[i]), seed=int(seeds[i]),
+                          params=PAR[i, :len(plan.params)]).estimates()
+        N = float(paths[i])
+        for k in range(plan.n_payoffs):
+            m, m_ref = s[i, k] / N, rs[0, k] / N
+            sd = math.sqrt(max(rq[0, k] / N - m_ref ** 2, 0.0))
+            if precision == "fp64":
+                assert abs(m - m_ref) <= 1e-9 * max(1.0, abs(m_ref), sd), (i, k, m, m_ref)
+            else:
+                # FP32: another checkpoint spacing and time arithmetic move
+                # each path by rounding only
+                assert abs(m - m_ref) <= 1e-4 * max(1.0, abs(m_ref), sd), (i, k, m, m_ref)
+        assert np.all(s[i, plan.n_payoffs:] == 0.0)
+
+
+def test_batched_adjoint_greeks_and_limits(engine):
+    """GBM instances of the batch against Black-Scholes delta / vega (Euler
+    at 365 steps, 2^16 paths each), and the step limit of the template."""
+    from sde_sim_rs.adjoint import black_scholes_call
+    from sde_sim_rs.batch import Batch
+    tg = engine.Plan(GBM_T, params=["mu", "sigma"], payoffs=["max(X - 100, 0)"], grad_params=["mu", "sigma"],
+                     grad_x0=["X"], precision="fp32", output="none")
+    sig = np.array([0.1, 0.2, 0.35, 0.5])
+    mu = np.array([0.0, 0.05, 0.02, -0.03])
+    n = len(sig)
+    b = Batch([tg])
+    job = b.prepare(np.zeros(n, np.int32), 365, 1.0, 1 << 16, np.arange(n, dtype=np.uint64) * 7919,
+                    np.full((n, 1), 100.0), np.stack([mu, sig], axis=1))
+    s, q = job.run().results()
+    N = float(1 << 16)
+    m = s / N
+    se = np.sqrt(np.maximum(q / N - m * m, 0) / N)
+    for i in range(n):
+        price, delta, vega, dmu = black_scholes_call(100.0, 100.0, sig[i], mu[i], 1.0)
+        for got, want, e in ((m[i, 0], price, se[i, 0]), (m[i, 3], delta, se[i, 3]), (m[i, 2], vega, se[i, 2]),
+                             (m[i, 1], dmu, se[i, 1])):
+            assert abs(got - want) < 4 * e + 5e-3 * abs(want), (i, got, want, e)
+    with pytest.raises(Exception, match="at most 4096 steps"):
+        b.prepare(np.zeros(1, np.int32), 4097, 1.0, 256, np.zeros(1, np.uint64), np.full((1, 1), 100.0),
+                  np.array([[0.05, 0.2]]))

@@ -28,6 +28,37 @@ def close64(gpu, ref):
     return float(np.nanmax(err)) if err.size else 0.0, int(bad.sum())
 
 
+# A jump count (dN) is the first k with F(k) >= u on the inversion walk of
+# src/proc/increment.rs:182-200.  The device's intensity or exp can differ
+# from the oracle's in the last bit; the count then flips only when u sits
+# within a few units of the last place of some F(k).  Every path that
+# differs from the oracle must show exactly that at its first divergent
+# step, in the oracle's own record of the draws there.
+FLIP_ULPS = 16
+
+
+def explain_jump_flips(oracle, eqs, gpu, ref, times, init, seed, n_per_replicate=0, **cfg):
+    """Asserts that every path differing from the oracle by more than the
+    FP64 bar diverges at a step where one of its Poisson draws lies within
+    FLIP_ULPS units of the last place of a CDF value; returns the report
+    [(path, step, ulps)]."""
+    bad = np.abs(gpu - ref) > FP64_RTOL * np.maximum(np.abs(ref), 1.0)
+    bad &= ~(np.isnan(gpu) & np.isnan(ref))
+    u = oracle.Universe(eqs)
+    report = []
+    for path in np.unique(np.nonzero(bad)[0]):
+        first_t = int(np.nonzero(bad[path].any(axis=-1))[0][0])
+        step = first_t - 1
+        assert step >= 0, (path, "differs at time 0")
+        draws = [d for d in u.jump_trace(times, init, int(path), seed=seed, n_per_replicate=n_per_replicate, **cfg)
+                 if d[0] == step]
+        assert draws, (path, step, "no Poisson draw at the first divergent step")
+        gap = min(oracle.poisson_boundary_ulps(d[2], d[3]) for d in draws)
+        assert gap <= FLIP_ULPS, (path, step, gap, draws)
+        report.append((int(path), step, gap))
+    return report
+
+
 # ---------------------------------------------------------------- KAT kernels
 
 @pytest.mark.parametrize("seed", [0, 42, 2**63 + 11, 2**64 - 1])
@@ -123,10 +154,10 @@ def test_fp64_paths_match_oracle(engine, oracle, case, scheme, rng, semantics):
                                         threads=THREADS, **_oracle_cfg(oracle, scheme, rng, semantics))
     err, nbad = close64(gpu, ref)
     if any("dN" in e for e in eqs):
-        # a jump count may flip when the FP64 intensity differs in its last
-        # bit at a CDF boundary; such a path then differs from that step on
-        paths_bad = np.unique(np.argwhere(np.abs(gpu - ref) > FP64_RTOL * np.maximum(np.abs(ref), 1))[:, 0])
-        assert len(paths_bad) <= 1, (err, paths_bad)
+        # a path may differ only through a jump count that flips at a CDF
+        # boundary (explained draw by draw from the oracle's record)
+        explain_jump_flips(oracle, eqs, gpu, ref, times, init, seed, n_per_replicate=n,
+                           **_oracle_cfg(oracle, scheme, rng, semantics))
     else:
         assert nbad == 0, err
 
@@ -153,13 +184,14 @@ def test_reference_examples_full_size(engine, oracle, name, eqs, init, times, sc
     gpu = plan.run(times, init, n, seed=seed).values("reference")[0]
     ref = oracle.Universe(eqs).simulate(times, init, 0, n, seed=seed, threads=THREADS,
                                         **_oracle_cfg(oracle, scheme, rng, "reference"))
-    bad = np.abs(gpu - ref) > FP64_RTOL * np.maximum(np.abs(ref), 1.0)
-    bad &= ~(np.isnan(gpu) & np.isnan(ref))
-    paths_bad = np.unique(np.argwhere(bad)[:, 0])
-    # jump counts can flip on a last-bit difference of the intensity at a
-    # CDF boundary (then that one path diverges); allow 0.1% of the paths
-    limit = 10 if any("dN" in e for e in eqs) else 0
-    assert len(paths_bad) <= limit, (name, len(paths_bad))
+    if any("dN" in e for e in eqs):
+        # every differing path is a jump count flipped at a CDF boundary
+        report = explain_jump_flips(oracle, eqs, gpu, ref, times, init, seed,
+                                    **_oracle_cfg(oracle, scheme, rng, "reference"))
+        print(f"{name}: {len(report)} of {n} paths diverge through a flipped jump count", report)
+    else:
+        err, nbad = close64(gpu, ref)
+        assert nbad == 0, (name, err)
 
 
 def test_replicates_and_offsets_are_scenario_ranges(engine, oracle):

@@ -135,3 +135,41 @@ def test_static_scratch_entry_refuses_tensor_core_plans(engine):
     rc = N.lib().sde_run_estimates_static(tc._h, times.ctypes.data, len(times), x0.ctypes.data, 4, None, 0,
                                           256, 1, 1, None, hs.ctypes.data, hq.ctypes.data)
     assert rc == N.SDE_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("tc", [False, True], ids=["cuda_cores", "tensor_cores"])
+def test_basket64_checkpoints_against_fp64_oracle(engine, oracle, tc):
+    """The 64-dimensional correlated basket at its own dimension: Euler,
+    XOR-scrambled Sobol (dimension 8192), 128 steps, FP32 output at 32
+    equally spaced checkpoints, against the FP64 oracle on the same points
+    (the per-term Euler sum of src/sim/euler.rs:15-28).  Every checkpoint
+    value of every path is compared."""
+    dim, n, seed = 64, 2048, 7
+    eqs, payoff, _, _ = basket_equations(dim)
+    times = np.linspace(0.0, 1.0, 129)
+    ck = list(range(4, 129, 4))
+    plan = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng="sobol", scramble="xor",
+                       output="checkpoints", tensor_cores=tc)
+    assert plan.uses_tensor_cores == tc
+    res = plan.run(times, _init(dim), n, seed=seed, checkpoints=ck)
+    gpu = res.values()[0]                                   # [path, checkpoint, process]
+    assert gpu.shape == (n, len(ck), dim)
+    u = oracle.Universe(eqs)
+    ref = u.simulate(times, _init(dim), 0, n, rng=oracle.SOBOL, scramble=oracle.XOR, seed=seed,
+                     n_per_replicate=n, full=True, threads=THREADS)[:, ck, :]
+    rel = np.abs(gpu - ref) / np.abs(ref)
+    # FP32 stepping against FP64 on the same inputs: 99% of all 4.2M values
+    # within 1e-3 relative (the FP32 bar); in practice all of them far inside
+    assert np.mean(rel < 1e-3) >= 0.99, np.percentile(rel, [50, 99, 100])
+    assert rel.max() < 1e-2, rel.max()
+    # per-process terminal means within 3 standard errors of the oracle's
+    for p in range(dim):
+        se = ref[:, -1, p].std() / math.sqrt(n)
+        assert abs(gpu[:, -1, p].mean() - ref[:, -1, p].mean()) <= 3 * se
+    # the basket call: the run's FP64 estimator against the oracle's payoff
+    # over the same paths
+    pay = u.payoff(payoff, 1.0, ref[:, -1, :])
+    s, q = res.estimates()
+    price = s[0, 0] / n
+    se = pay.std() / math.sqrt(n)
+    assert abs(price - pay.mean()) <= max(3 * se * 1e-2, 1e-4 * abs(pay.mean())) + 1e-12, (price, pay.mean(), se)

@@ -168,3 +168,27 @@ def test_icdf_accurate_option(oracle):
     got = np.array([oracle.icdf_accurate(float(x)) for x in p])
     want = sp.ndtri(p)
     assert np.max(np.abs(got - want) / np.maximum(np.abs(want), 1.0)) < 2e-15
+
+
+def test_jump_trace_and_cdf_boundaries(oracle):
+    """The oracle's record of Poisson draws: one draw per dN term and step in
+    the reference's order, each count the inversion walk's; a draw on a CDF
+    value is 0 units of the last place from it, and there a last-bit change
+    of lambda * dt moves the count, while typical draws sit far away."""
+    times = np.arange(0.0, 3.0, 0.1)
+    u = oracle.Universe(EXAMPLE_PY)
+    tr = u.jump_trace(times, {"X0": 0.5, "X1": 100.0, "X2": 0.0}, 5, scheme=oracle.RK, seed=9)
+    # dN1 appears in two terms (X0 and X1): two draws per step, same uniform
+    assert len(tr) == 2 * (len(times) - 1)
+    for (t, idx, uu, lam, k), (t2, _, uu2, _, _) in zip(tr[0::2], tr[1::2]):
+        assert idx == 0 and t == t2 and uu == uu2
+        assert k == oracle.poisson(uu, lam)
+    gaps = [oracle.poisson_boundary_ulps(d[2], d[3]) for d in tr]
+    assert min(gaps) > 1e6
+    # a uniform placed on F(1): the walk stops at k = 1 for lambda and moves
+    # to 2 when lambda shrinks by a few units of its last place
+    lam = 0.37
+    f1 = math.exp(-lam) * (1.0 + lam)
+    assert oracle.poisson_boundary_ulps(f1, lam) <= 1.0
+    counts = {oracle.poisson(f1, lam * (1 + j * 2.0 ** -52)) for j in range(-8, 9)}
+    assert counts == {1, 2}
