@@ -661,68 +661,121 @@ def run_basket(args):
                           "tensor_cores": v["tc"]} for k, v in legs.items()}})
 
 
-def run_batched(args):
+def batched_legs(args, stream, flush):
     """4096 uneven GBM / OU instances in one persistent graph-captured launch
-    (FP32), against 4096 plain per-instance FP64 launches."""
+    (FP32): the forward batch, and the forward+adjoint batch (gradients of
+    E[X_T] with respect to every parameter and X0), each against 4096 plain
+    per-instance FP64 forward launches on the same paths."""
     import numpy as np
     import torch
     import sde_sim_rs
     from sde_sim_rs.batch import Batch
     tid, steps, paths, seeds, x0, params = batched_instances(n=args.instances)
-    tg = sde_sim_rs.Plan(GBM_P, params=["mu", "sigma"], payoffs=["X"], precision="fp32", output="none")
-    to = sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], precision="fp32", output="none")
-    stream = torch.cuda.current_stream()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    t0 = time.perf_counter()
-    job = Batch([tg, to]).prepare(tid, steps, 1.0, paths, seeds, x0, params, autotune=True, stream=stream)
-    prep_s = time.perf_counter() - t0
-    for _ in range(args.warmup):
-        job.run(stream).results()
-    with Clocks(0) as clk:
-        ms, _ = _timed_runs(lambda: job.run(stream), args.steps, stream, flush)
-    ms_step = sum(ms) / len(ms)
-    ps = job.path_steps
-    s, q = job.results()
-    t0 = time.perf_counter()
-    for _ in range(3):
-        job.run(stream).results()
-    e2e_s = (time.perf_counter() - t0) / 3
-    # baseline: plain per-instance FP64 launches
+    fwd_t = [sde_sim_rs.Plan(GBM_P, params=["mu", "sigma"], payoffs=["X"], precision="fp32", output="none"),
+             sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], precision="fp32", output="none")]
+    adj_t = [sde_sim_rs.Plan(GBM_P, params=["mu", "sigma"], payoffs=["X"], grad_params=["mu", "sigma"],
+                             grad_x0=["X"], precision="fp32", output="none"),
+             sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], grad_params=["theta", "m", "s"],
+                             grad_x0=["X"], precision="fp32", output="none")]
+    # baseline: plain per-instance FP64 forward launches
     pg = sde_sim_rs.Plan(GBM_P, params=["mu", "sigma"], payoffs=["X"], precision="fp64", output="none")
     po = sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], precision="fp64", output="none")
+    ps = int(np.sum(steps.astype(np.uint64) * paths))
+
+    def fp64_launches():
+        res = []
+        for i in range(len(tid)):
+            plan = pg if tid[i] == 0 else po
+            res.append(plan.run(np.arange(steps[i] + 1) / steps[i], {"X": x0[i, 0]}, int(paths[i]),
+                                seed=int(seeds[i]), params=params[i, :len(plan.params)], stream=stream))
+        return res
+    fp64_launches()[-1].wait()   # warm: both plans loaded
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res = []
-    for i in range(len(tid)):
-        plan = pg if tid[i] == 0 else po
-        res.append(plan.run(np.arange(steps[i] + 1) / steps[i], {"X": x0[i, 0]}, int(paths[i]), seed=int(seeds[i]),
-                            params=params[i, :len(plan.params)], stream=stream))
+    res = fp64_launches()
     torch.cuda.synchronize()
     fp64_s = time.perf_counter() - t0
-    z = []
+    m64 = np.zeros(len(tid))
+    se64 = np.zeros(len(tid))
     for i, r in enumerate(res):
         rs, rq = r.estimates()
         N = float(paths[i])
-        m64 = rs[0, 0] / N
-        se = math.sqrt(max(rq[0, 0] / N - m64 ** 2, 0) / N)
-        z.append(abs(s[i, 0] / N - m64) / max(se, 1e-300))
-    z = np.array(z)
-    _common(args, f"batched_{len(tid)}_gbm_ou_fp32", f"path-steps/s (fwd, {len(tid)} batched instances, FP32)",
-            ps / (ms_step * 1e-3), ms_step, "f32", clk.summary(),
-            {"value": ps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
-             "d2h_bytes_per_step": len(tid) * 16, "note": "graph replay + results read back"},
+        m64[i] = rs[0, 0] / N
+        se64[i] = math.sqrt(max(rq[0, 0] / N - m64[i] ** 2, 0) / N)
+    thr64 = ps / fp64_s
+
+    out = {}
+    for leg, templates in (("forward", fwd_t), ("fwd_adjoint", adj_t)):
+        t0 = time.perf_counter()
+        job = Batch(templates).prepare(tid, steps, 1.0, paths, seeds, x0, params, autotune=True, stream=stream)
+        prep_s = time.perf_counter() - t0
+        for _ in range(args.warmup):
+            job.run(stream).results()
+        with Clocks(0) as clk:
+            ms, _ = _timed_runs(lambda: job.run(stream), args.steps, stream, flush)
+        ms_step = statistics.median(ms)
+        s, q = job.results()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            job.run(stream).results()
+        e2e_s = (time.perf_counter() - t0) / 3
+        m32 = s[:, 0] / paths
+        bias = m32 - m64
+        z = np.abs(bias) / np.maximum(se64, 1e-300)
+        thr = ps / (ms_step * 1e-3)
+        # equal RMSE per instance (RMSE^2 = se^2 N/N' + bias^2), weighted by
+        # each instance's share of the path-steps
+        w = steps.astype(np.float64) * paths / ps
+        frac = float(np.sum(w * np.clip(1.0 - (bias / np.maximum(se64, 1e-300)) ** 2, 0.0, None)))
+        out[leg] = {"path_steps_per_s": thr, "ms": ms_step, "e2e_path_steps_per_s": ps / e2e_s, "prepare_s": prep_s,
+                    "block": job.block, "paths_per_thread": job.paths_per_thread, "work_items": job.n_items,
+                    "estimates_per_instance": job.n_payoffs, "clocks": clk.summary(),
+                    "throughput_ratio_vs_fp64_launches": thr / thr64,
+                    "equal_rmse_speedup_vs_fp64_launches": thr / thr64 * frac,
+                    "fraction_within_3se_of_fp64": float(np.mean(z < 3)), "max_abs_z_vs_fp64": float(z.max())}
+        if leg == "fwd_adjoint":
+            # gradient of E[X_T] in X0 under Euler with n uniform steps:
+            # (1 + mu/n)^n for GBM, (1 - theta/n)^n for OU (exact for the
+            # discrete recursion; the OU one has no Monte Carlo error)
+            g = tid == 0
+            col = np.where(g, 3, 4)   # [payoff, (mu, sigma) | (theta, m, s), X0]
+            rows = np.arange(len(tid))
+            dx = s[rows, col] / paths
+            dx_se = np.sqrt(np.maximum(q[rows, col] / paths - dx ** 2, 0) / paths)
+            want = np.where(g, (1.0 + params[:, 0] / steps) ** steps, (1.0 - params[:, 0] / steps) ** steps)
+            out[leg]["dX0_within_4se_of_discrete_closed_form"] = float(
+                np.mean(np.abs(dx - want) <= 4 * dx_se + 1e-4 * np.abs(want)))
+    out["fp64_per_instance_launches"] = {"path_steps_per_s": thr64, "seconds": fp64_s, "launches": int(len(tid))}
+    out["config"] = {"instances": int(len(tid)), "path_steps": ps,
+                     "adjoint": "gradients of E[X_T] in (mu, sigma, X0) for GBM and (theta, m, s, X0) for OU; "
+                                "checkpoints every ceil(sqrt(steps)) steps, increments drawn again",
+                     "path_steps_counted": "forward path-steps (paths x steps) for both legs"}
+    return out
+
+
+def run_batched(args):
+    """4096 uneven GBM / OU instances in one persistent graph-captured launch
+    (FP32), forward and forward+adjoint, against 4096 plain per-instance FP64
+    forward launches."""
+    import torch
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = batched_legs(args, stream, flush)
+    f = out["forward"]
+    clocks = f.pop("clocks")
+    out["fwd_adjoint"].pop("clocks")
+    _common(args, f"batched_{out['config']['instances']}_gbm_ou_fp32",
+            f"path-steps/s (fwd, {out['config']['instances']} batched instances, FP32)",
+            f["path_steps_per_s"], f["ms"], "f32", clocks,
+            {"value": f["e2e_path_steps_per_s"], "unit": "path-steps/s", "h2d_bytes_per_step": 0,
+             "d2h_bytes_per_step": out["config"]["instances"] * 16, "note": "graph replay + results read back"},
             2 * args.steps,
             # one Wiener index per instance: one u64 per path-step, 1/8 block
-            _chacha_roofline(ps / (ms_step * 1e-3), 1.0 / 8.0,
+            _chacha_roofline(f["path_steps_per_s"], 1.0 / 8.0,
                              "each path-step draws one u64 of its scenario's ChaCha8 stream",
                              # ncu (1 pass, the full 4096 instances): 3.48 MB read, 0 B written
                              3.48e6),
-            None,
-            {"instances": len(tid), "path_steps": ps, "block": job.block, "paths_per_thread": job.paths_per_thread,
-             "work_items": job.n_items, "prepare_s": prep_s,
-             "fp64_per_instance_launches": {"value": ps / fp64_s, "unit": "path-steps/s", "seconds": fp64_s},
-             "speedup_vs_fp64_launches": (ps / (ms_step * 1e-3)) / (ps / fp64_s),
-             "fraction_within_3se_of_fp64": float(np.mean(z < 3)), "max_z": float(z.max())})
+            None, out)
 
 
 ADJ_MODELS = (

@@ -325,6 +325,16 @@ int sde_kat_icdf(const double* host_p, uint64_t n, double* host_out);
 /* Host-side Joe-Kuo direction numbers [dims][32] (no GPU needed). */
 int sde_sobol_directions(int32_t dims, uint32_t* host_out);
 
+/* ---- test hook -----------------------------------------------------------
+ * No counterpart in the reference.  Sets, for runs launched afterwards from
+ * any thread, how many SM clocks the tensor-core step with several threads
+ * per path waits for its A operand before it gives up (0 restores the
+ * default of about 1 s; a short budget polls without suspending).  A run
+ * that gave up stops stepping, waits with the full budget for its copies
+ * and product in flight, frees its tensor memory and reports SDE_ERR_DEVICE
+ * from sde_result_wait; the plan stays usable.  For tests of that path.  */
+int sde_debug_tc_wait_cycles(uint64_t cycles);
+
 /* ---- measurement helper ------------------------------------------------
  * Times a kernel that keeps the SFU (MUFU) pipe busy and reports its
  * throughput in operations per second; the roofline denominator of the

@@ -281,6 +281,17 @@ struct Gen {
         if (xorm()) return 32 / std::gcd(NI, 32);
         return 8 / std::gcd(NI, 8);
     }
+    // The FP32 forward CUDA-core kernel on the reference's shifted Sobol
+    // points, with a power-of-two number of stochastic indices up to 32: an
+    // outer loop over 32-dimension chunks (32 / NI steps) fetches the warp's
+    // two high parts once per chunk, and the inner step groups (whole
+    // ChaCha8 blocks, a rolled loop) find their shuffle lanes and LO words
+    // at an offset eo from the chunk's start.  Other kernels check per
+    // dimension whether the chunk changed.
+    bool grp_shift = false;
+    bool grp_shift_eligible() const {
+        return shiftm() && f32 && !mma && NI > 0 && NI <= 32 && (NI & (NI - 1)) == 0;
+    }
     // the FP32 XOR path goes straight from the scrambled word to a normal;
     // q / up / gt are formed only where a jump count or RK's sign needs them
     bool needs_tail(int k) const {
@@ -310,7 +321,7 @@ struct Gen {
     // ---- uniforms of step t for the current lane ------------------------
     // Forward / batch kernels: step groups of U steps hold whole ChaCha
     // blocks in registers (indices known at compile time).
-    void uniform_from(Out& o, int k) const {
+    void uniform_from(Out& o, int k, int g = -1) const {
         const std::string K = S(k);
         // FP32: the 53-bit uniform U (p = U 2^-53); the tail q / up / gt
         // only where a jump count, RK's sign or the accurate icdf reads it
@@ -326,6 +337,30 @@ struct Gen {
                 o.l("const sde_u64 " + V("U", k) + " = " + V("r", k) + " >> 11;");
                 tail53();
             }
+        } else if (shiftm() && grp_shift && g >= 0) {
+            // dimension t*NI + k = chunk start + eo + e (eo: the step
+            // group's offset in the chunk, a multiple of 4 or of the group's
+            // dimensions): the chunk's high parts and this lane's LO words
+            // in loads of lo_width() dimensions
+            const int e = g * NI + k;
+            const int lw = lo_width(), e0 = e - e % lw;
+            const std::string at = S((e0 / 4) * 128 + e0 % 4);
+            std::string word;
+            if (lw == 1) {
+                word = "__ldg(" + V("LOp") + " + " + at + ")";
+            } else {
+                if (e % lw == 0)
+                    o.l("const uint" + S(lw) + " " + V("LW", e) + " = __ldg((const uint" + S(lw) + "*)(" + V("LOp") + " + " +
+                        at + "));");
+                static const char* const comp[4] = {"x", "y", "z", "w"};
+                word = V("LW", e0) + "." + comp[e % lw];
+            }
+            o.l("const sde_u32 " + V("sa", k) + " = __shfl_sync(0xffffffffu, " + V("sh0") + ", eo + " + S(e) + ");");
+            o.l("const sde_u32 " + V("sb", k) + " = __shfl_sync(0xffffffffu, " + V("sh1") + ", eo + " + S(e) + ");");
+            o.l("const sde_u32 " + V("x", k) + " = (" + V("shi1") + " ? " + V("sb", k) + " : " + V("sa", k) + ") ^ " + word +
+                ";");
+            o.l("const sde_u64 " + V("U", k) + " = sde_shift_u53(" + V("x", k) + ", " + V("r", k) + ");");
+            tail53();
         } else if (shiftm()) {
             // the dimension's point from the warp's two high parts (fetched
             // once per 32 dimensions) and this lane's low part
@@ -414,7 +449,7 @@ struct Gen {
                 o.l("const sde_u64 " + V("r", k) + " = sde_pair(" + V("B", b) + "[" + S(w) + "], " + V("B", b) + "[" +
                     S(w + 1) + "]);");
             }
-            uniform_from(o, k);
+            uniform_from(o, k, g);
         }
     }
 
@@ -453,7 +488,7 @@ struct Gen {
                 // one reciprocal for the pair where the SFU pipe is the
                 // bound (the CUDA-core kernels); one each in the tensor-core
                 // step, which is bound by issue (measured both ways)
-                const std::string tpl = mma ? "<false>(" : "(";
+                const std::string tpl = mma ? "<false>(" : shiftm() ? "<true, true>(" : "(";
                 const std::string src = xorm() ? "sde_normal_xor2" + tpl + V("y", ka) + ", " + V("y", kb) + ")"
                                                 : "sde_normal_u53_2" + tpl + V("U", ka) + ", " + V("U", kb) + ")";
                 o.l("const float2 " + pr + " = __fmul2_rn(make_float2(" + mult + ", " + mult + "), " + src + ");");
@@ -740,7 +775,7 @@ struct Gen {
             o.l("sde_mbar_arrive(ABAR);");
             if (half == 0) {
                 o.l("if (threadIdx.x < 32) {");
-                o.l("  const bool a_ready = sde_mbar_wait_bounded(ABAR, tc_phase);");
+                o.l("  const bool a_ready = sde_mbar_wait_budget(ABAR, tc_phase, a.tc_wait_cycles);");
                 o.l("  if (!a_ready) tc_ok = 0;");
                 o.l("  if (threadIdx.x == 0 && a_ready) {");
                 o.l("    sde_tc_fence_after();");
@@ -1097,7 +1132,28 @@ struct Gen {
             }
             lane(0);
         }
-        o.l("for (int t0 = 0; t0 < n_steps; t0 += " + S(U) + ") {");
+        if (grp_shift) {
+            // a 32-dimension chunk: its high parts for the warp's two point
+            // groups, then its step groups in a rolled loop
+            const int OS = 32 / NI;
+            o.l("for (int t1 = 0; t1 < n_steps; t1 += " + S(OS) + ") {");
+            o.ind++;
+            o.l("const int chunk0 = (t1 * " + S(NI) + ") >> 5;");
+            for (int j = 0; j < ppt; ++j) {
+                lane(j);
+                o.l("const sde_u32 " + V("sh0") + " = sde_sobol_hi_unrolled(a.sobol_vt, nullptr, a.sobol_dims, chunk0, " +
+                    V("sH0") + ", lane);");
+                o.l("const sde_u32 " + V("sh1") + " = sde_sobol_hi_unrolled(a.sobol_vt, nullptr, a.sobol_dims, chunk0, " +
+                    V("sH1") + ", lane);");
+                o.l("const sde_u32* " + V("LOp1") + " = a.sobol_lo + (sde_u64)t1 * " + S(NI * 32) + "u + " + V("sL") +
+                    " * 4u;");
+            }
+            lane(0);
+            o.l("#pragma unroll 1");
+            o.l("for (int t0 = t1; t0 < min(t1 + " + S(OS) + ", n_steps); t0 += " + S(U) + ") {");
+        } else {
+            o.l("for (int t0 = 0; t0 < n_steps; t0 += " + S(U) + ") {");
+        }
         o.ind++;
         if (uses_chacha()) {
             o.l("const sde_u64 blk0 = ((sde_u64)t0 * " + S(NI) + "ull) / 8ull;");
@@ -1120,6 +1176,15 @@ struct Gen {
                 // while the product runs
                 if (hv_pf() && !mma) hv_prefetch(o, "chunk0 + " + S(nblocks));
             }
+        }
+        if (grp_shift) {
+            // the step group's dimensions from offset eo of the chunk
+            o.l("const int eo = (t0 - t1) * " + S(NI) + ";");
+            for (int j = 0; j < ppt; ++j) {
+                lane(j);
+                o.l("const sde_u32* " + V("LOp") + " = " + V("LOp1") + " + (eo >> 2) * 128;");
+            }
+            lane(0);
         }
         // a full group (every group but perhaps the last) runs its steps
         // without the per-step bound check: forward CUDA-core kernels on
@@ -1159,6 +1224,10 @@ struct Gen {
         if (full_copy) o.l("}");
         o.ind--;
         o.l("}");
+        if (grp_shift) {
+            o.ind--;
+            o.l("}");
+        }
         lane(0);
     }
 
@@ -1180,6 +1249,7 @@ struct Gen {
 
     std::string forward(const std::string& name) {
         mode = Mode::Forward;
+        grp_shift = grp_shift_eligible();
         const int K = (int)sp.payoffs.size();
         Out o;
         o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
@@ -1200,6 +1270,7 @@ struct Gen {
         }
         o.ind--;
         o.l("}");
+        grp_shift = false;
         return o.s.str();
     }
 

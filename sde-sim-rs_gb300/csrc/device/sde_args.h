@@ -45,6 +45,9 @@ typedef struct sde_args {
     float udt_f, usdt_f;      /* the FP32 step and its square root when every
                                  step of the grid has them (uniform-grid kernels) */
     int pad1;
+    sde_u64 tc_wait_cycles;   /* tensor-core step, several threads per path: SM
+                                 clocks the A-ready wait lasts before it gives up
+                                 (0: about 1 s, the other waits' budget)         */
 } sde_args;
 
 /* ---- batched instances: many independent SDE instances in one persistent

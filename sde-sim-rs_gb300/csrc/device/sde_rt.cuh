@@ -192,11 +192,23 @@ SDE_DEV float2 sde_normal_xor2(sde_u32 ya, sde_u32 yb) {
                        __int_as_float(__float_as_int(x.y) ^ (~sb & 0x80000000u)));
 }
 
-template <bool SHARED = true>
+/* float of a tail integer Q <= 2^52 from its two 32-bit halves: hi < 2^21
+ * converts exactly, lo rounds by at most 2^7, and the FMA rounds once; within
+ * one ulp of the correctly rounded value, without the 64-bit conversion,
+ * which runs on the FP64 pipe */
+SDE_DEV float sde_q53_to_float(sde_u64 Q) {
+    return fmaf(__uint2float_rn((sde_u32)(Q >> 32)), 0x1p32f, __uint2float_rn((sde_u32)Q));
+}
+
+/* SPLIT_CVT: the tails convert with sde_q53_to_float (the shifted-Sobol
+ * kernels, where the FP64 pipe is busy); else one 64-bit conversion each
+ * (the ChaCha8 kernels, bound by issue, measured slower with the split) */
+template <bool SHARED = true, bool SPLIT_CVT = false>
 SDE_DEV float2 sde_normal_u53_2(sde_u64 Ua, sde_u64 Ub) {
     const bool upa = Ua >= (1ull << 52), upb = Ub >= (1ull << 52);
     const sde_u64 Qa = upa ? (1ull << 53) - Ua : Ua, Qb = upb ? (1ull << 53) - Ub : Ub;
-    const float2 lg = make_float2(sde_lg2_approx(__ull2float_rn(Qa)), sde_lg2_approx(__ull2float_rn(Qb)));
+    const float2 lg = SPLIT_CVT ? make_float2(sde_lg2_approx(sde_q53_to_float(Qa)), sde_lg2_approx(sde_q53_to_float(Qb)))
+                                : make_float2(sde_lg2_approx(__ull2float_rn(Qa)), sde_lg2_approx(__ull2float_rn(Qb)));
     const float2 x = sde_as26_abs2<SHARED>(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
                                                       make_float2(73.473601139354201f, 73.473601139354201f)));
     return make_float2(upa ? x.x : -x.x, upb ? x.y : -x.y);
@@ -360,6 +372,26 @@ SDE_DEV bool sde_mbar_wait_bounded(sde_u32 mbar, sde_u32 parity) {
     const long long t0 = clock64();
     while (!sde_mbar_try_wait(mbar, parity))
         if (clock64() - t0 > 2000000000ll) return false;
+    return true;
+}
+/* the phase's state now, without suspending */
+SDE_DEV bool sde_mbar_test_wait(sde_u32 mbar, sde_u32 parity) {
+    sde_u32 ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+/* sde_mbar_wait_bounded with a budget of `cycles` SM clocks (0: the ~1 s
+ * default); a shorter budget polls without suspending, so it gives up once
+ * the budget is spent even when the phase would complete soon after */
+SDE_DEV bool sde_mbar_wait_budget(sde_u32 mbar, sde_u32 parity, sde_u64 cycles) {
+    if (cycles == 0ull) return sde_mbar_wait_bounded(mbar, parity);
+    const long long t0 = clock64();
+    while (!sde_mbar_test_wait(mbar, parity))
+        if (clock64() - t0 > (long long)cycles) return false;
     return true;
 }
 /* one arrival (release) on a CTA mbarrier */

@@ -40,6 +40,10 @@ namespace sde {
 // ---------------------------------------------------------------------------
 
 static thread_local std::string g_last_error;
+// Budget of the tensor-core step's A-ready wait in SM clocks for runs
+// launched from now on (0: the default of about 1 s); set only by
+// sde_debug_tc_wait_cycles, a test hook.
+static std::atomic<unsigned long long> g_tc_wait_cycles{0ull};
 
 struct Error {
     int code;
@@ -709,6 +713,7 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
         *r->status_host.as<int>() = 0;
         cuda_check(cudaMemsetAsync(r->status.p, 0, 16, r->stream), "status word");
         A.status = r->status.as<int>();
+        A.tc_wait_cycles = g_tc_wait_cycles.load(std::memory_order_relaxed);
     }
 
     if (N > 0 && T >= 1) {
@@ -761,6 +766,11 @@ using namespace sde;
 extern "C" {
 
 int32_t sde_abi_version(void) { return SDE_ABI_VERSION; }
+
+int sde_debug_tc_wait_cycles(uint64_t cycles) {
+    g_tc_wait_cycles.store(cycles, std::memory_order_relaxed);
+    return SDE_OK;
+}
 
 int sde_last_error(char* buf, size_t n) {
     if (!buf || n == 0) return SDE_ERR_INVALID;

@@ -70,6 +70,7 @@ class SdeError(RuntimeError):
 SIGNATURES = {
     "sde_abi_version": ([], C.c_int32),
     "sde_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
+    "sde_debug_tc_wait_cycles": ([C.c_uint64], C.c_int),
     "sde_options_init": ([C.POINTER(Options)], None),
     "sde_run_args_init": ([C.POINTER(RunArgs)], None),
     "sde_plan_create": ([C.POINTER(C.c_char_p), C.c_int32, C.POINTER(C.c_char_p), C.c_int32,

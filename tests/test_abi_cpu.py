@@ -59,7 +59,7 @@ def test_lowering_compiles(engine, scheme, rng, scramble, precision, semantics):
     assert "__global__" in src and "sde_step_" in src
     if precision == "fp32":
         # FP32 stepping: no double arithmetic in the step body
-        body = src.split("for (int t0 = 0;")[1].split("double fs[")[0]
+        body = re.split(r"for \(int t[01] = 0;", src)[1].split("double fs[")[0]
         assert "double" not in body
 
 

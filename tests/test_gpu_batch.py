@@ -130,7 +130,7 @@ def test_batched_adjoint_matches_per_instance_adjoint_runs(engine, precision):
     templates = _adjoint_templates(engine, precision)
     job = Batch(templates).prepare(tid, steps, 1.0, paths, seeds, X0, PAR)
     s, q = job.run().results()
-    assert s.shape == (n, 6)   # GBM: 2 payoffs + 3 gradients; widest template
+    assert s.shape == (n, 5)   # the widest templates: GBM 2 payoffs + 3 gradients, OU and Heston 1 + 4
     for i in range(n):
         plan = templates[tid[i]]
         times = np.arange(steps[i] + 1) / steps[i]

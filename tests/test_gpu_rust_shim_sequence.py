@@ -27,9 +27,10 @@ def _shim_simulate(lib, eqs, times, init, n, scheme, rng, seed=None):
     names = list(init)
     vals = np.array([init[k] for k in names] or [0.0], dtype=np.float64)
     r = C.c_void_p()
-    rc = lib.sde_simulate(_cstrs(eqs), len(eqs), t.ctypes.data, len(t), _cstrs(names), vals.ctypes.data,
-                          len(names), n, scheme.encode(), rng.encode(), 0 if seed is None else seed,
-                          0 if seed is None else 1, C.byref(r))
+    dp = C.POINTER(C.c_double)
+    rc = lib.sde_simulate(_cstrs(eqs), len(eqs), t.ctypes.data_as(dp), len(t), _cstrs(names),
+                          vals.ctypes.data_as(dp), len(names), n, scheme.encode(), rng.encode(),
+                          0 if seed is None else seed, 0 if seed is None else 1, C.byref(r))
     if rc != 0:
         buf = C.create_string_buffer(4096)
         lib.sde_last_error(buf, len(buf))

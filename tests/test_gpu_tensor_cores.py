@@ -173,3 +173,30 @@ def test_basket64_checkpoints_against_fp64_oracle(engine, oracle, tc):
     price = s[0, 0] / n
     se = pay.std() / math.sqrt(n)
     assert abs(price - pay.mean()) <= max(3 * se * 1e-2, 1e-4 * abs(pay.mean())) + 1e-12, (price, pay.mean(), se)
+
+
+def test_tensor_core_wait_that_runs_out_is_reported(engine):
+    """The A-ready wait of the two-threads-per-path step, given a budget of
+    four clocks (polling, no suspend), gives up at some step of some CTA.
+    That CTA stops stepping, waits with the full budget for its copies and
+    product in flight, frees its tensor memory and sets the status word:
+    the run reports SDE_ERR_DEVICE.  The next run on the same plan, with the
+    default budget, matches the CUDA-core kernel.  Nothing faults: every wait
+    is bounded."""
+    from sde_sim_rs import _native as N
+    dim = 64
+    eqs, payoff, _, _ = basket_equations(dim)
+    tc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng="sobol", scramble="xor", tensor_cores=True)
+    cc = engine.Plan(eqs, payoffs=[payoff], precision="fp32", rng="sobol", scramble="xor")
+    times = np.linspace(0.0, 1.0, 33)
+    tc.run(times, _init(dim), 256, seed=5).wait()
+    N.check(N.lib().sde_debug_tc_wait_cycles(4))
+    try:
+        with pytest.raises(N.SdeError) as e:
+            tc.run(times, _init(dim), 256, seed=5).wait()
+        assert e.value.code == N.SDE_ERR_DEVICE and "timed out" in str(e.value)
+    finally:
+        N.check(N.lib().sde_debug_tc_wait_cycles(0))
+    a = tc.run(times, _init(dim), 1000, replicates=2, seed=5).values()
+    b = cc.run(times, _init(dim), 1000, replicates=2, seed=5).values()
+    assert np.max(np.abs(a - b) / np.abs(b)) < 2e-5
