@@ -40,7 +40,7 @@ def _write_if_changed(path: str, text: str) -> None:
 
 def gen_embedded() -> None:
     out = ["// generated by build.py -- do not edit", "#pragma once"]
-    for name, rel in (("kEmbArgs", "device/sde_args.h"), ("kEmbLog", "device/sde_log.h"), ("kEmbChacha", "device/sde_chacha.h"),
+    for name, rel in (("kEmbArgs", "device/sde_args.h"), ("kEmbLog", "device/sde_log.h"), ("kEmbChacha", "device/sde_chacha.h"), ("kEmbShift", "device/sde_shift.h"),
                       ("kEmbRt", "device/sde_rt.cuh")):
         with open(os.path.join(HERE, rel)) as f:
             text = f.read()
@@ -94,7 +94,7 @@ def build(verbose: bool = False) -> str:
     cuda = cuda_home()
     inc = ["-I" + os.path.join(cuda, "include"), "-I" + HERE]
     headers = [os.path.join(HERE, h) for h in
-               ("frontend.h", "codegen.h", "kernels.h", "device/sde_args.h", "device/sde_log.h", "device/sde_chacha.h", "device/sde_rt.cuh",
+               ("frontend.h", "codegen.h", "kernels.h", "device/sde_args.h", "device/sde_log.h", "device/sde_chacha.h", "device/sde_shift.h", "device/sde_rt.cuh",
                 "_gen/embedded.h", "_gen/joe_kuo_d6.h")]
     headers.append(os.path.normpath(os.path.join(HERE, "..", "..", "include", "sdegpu.h")))
     jobs = []

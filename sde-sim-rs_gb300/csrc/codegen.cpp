@@ -359,7 +359,11 @@ struct Gen {
             o.l("const sde_u32 " + V("sb", k) + " = __shfl_sync(0xffffffffu, " + V("sh1") + ", eo + " + S(e) + ");");
             o.l("const sde_u32 " + V("x", k) + " = (" + V("shi1") + " ? " + V("sb", k) + " : " + V("sa", k) + ") ^ " + word +
                 ";");
-            o.l("const sde_u64 " + V("U", k) + " = sde_shift_u53(" + V("x", k) + ", " + V("r", k) + ");");
+            // U = uh 2^21 + ul in 32-bit pieces (the 64-bit U only where a
+            // single normal, a jump count or RK's sign reads it)
+            o.l("sde_u32 " + V("uh", k) + ", " + V("ul", k) + "; sde_shift_split(" + V("x", k) + ", " + V("r", k) + ", &" +
+                V("uh", k) + ", &" + V("ul", k) + ");");
+            o.l("const sde_u64 " + V("U", k) + " = ((sde_u64)" + V("uh", k) + " << 21) | " + V("ul", k) + ";");
             tail53();
         } else if (shiftm()) {
             // the dimension's point from the warp's two high parts (fetched
@@ -490,7 +494,9 @@ struct Gen {
                 // step, which is bound by issue (measured both ways)
                 const std::string tpl = mma ? "<false>(" : shiftm() ? "<true, true>(" : "(";
                 const std::string src = xorm() ? "sde_normal_xor2" + tpl + V("y", ka) + ", " + V("y", kb) + ")"
-                                                : "sde_normal_u53_2" + tpl + V("U", ka) + ", " + V("U", kb) + ")";
+                                        : grp_shift ? "sde_normal_split2(" + V("uh", ka) + ", " + V("ul", ka) + ", " +
+                                                          V("uh", kb) + ", " + V("ul", kb) + ")"
+                                                    : "sde_normal_u53_2" + tpl + V("U", ka) + ", " + V("U", kb) + ")";
                 o.l("const float2 " + pr + " = __fmul2_rn(make_float2(" + mult + ", " + mult + "), " + src + ");");
                 o.l("const float " + V("w", ka) + " = " + pr + ".x;");
                 o.l("const float " + V("w", kb) + " = " + pr + ".y;");

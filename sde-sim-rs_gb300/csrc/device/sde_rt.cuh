@@ -24,6 +24,7 @@
  * kernels' source, included here for the nvcc-built ones) */
 #ifndef SDE_CHACHA_H
 #include "sde_chacha.h"
+#include "sde_shift.h"
 #endif
 
 SDE_DEV sde_u64 sde_pair(sde_u32 lo, sde_u32 hi) { return ((sde_u64)hi << 32) | (sde_u64)lo; }
@@ -209,6 +210,24 @@ SDE_DEV float2 sde_normal_u53_2(sde_u64 Ua, sde_u64 Ub) {
     const sde_u64 Qa = upa ? (1ull << 53) - Ua : Ua, Qb = upb ? (1ull << 53) - Ub : Ub;
     const float2 lg = SPLIT_CVT ? make_float2(sde_lg2_approx(sde_q53_to_float(Qa)), sde_lg2_approx(sde_q53_to_float(Qb)))
                                 : make_float2(sde_lg2_approx(__ull2float_rn(Qa)), sde_lg2_approx(__ull2float_rn(Qb)));
+    const float2 x = sde_as26_abs2<SHARED>(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
+                                                      make_float2(73.473601139354201f, 73.473601139354201f)));
+    return make_float2(upa ? x.x : -x.x, upb ? x.y : -x.y);
+}
+
+/* Two normals of the reference's shifted Sobol uniforms U = hi 2^21 + lo
+ * (sde_shift_split): the tails Q = hq 2^21 + lq in 32-bit pieces
+ * (sde_tail_split), float(Q) = fma(float(hq), 2^21, float(lq)) within one
+ * ulp (hq <= 2^31 rounds once, lq < 2^21 is exact), then as
+ * sde_normal_u53_2. */
+template <bool SHARED = true>
+SDE_DEV float2 sde_normal_split2(sde_u32 ha, sde_u32 la, sde_u32 hb, sde_u32 lb) {
+    sde_u32 qha, qla, qhb, qlb;
+    int upa, upb;
+    sde_tail_split(ha, la, &qha, &qla, &upa);
+    sde_tail_split(hb, lb, &qhb, &qlb, &upb);
+    const float2 lg = make_float2(sde_lg2_approx(fmaf(__uint2float_rn(qha), 0x1p21f, __uint2float_rn(qla))),
+                                  sde_lg2_approx(fmaf(__uint2float_rn(qhb), 0x1p21f, __uint2float_rn(qlb))));
     const float2 x = sde_as26_abs2<SHARED>(__ffma2_rn(lg, make_float2(-1.3862943611198906f, -1.3862943611198906f),
                                                       make_float2(73.473601139354201f, 73.473601139354201f)));
     return make_float2(upa ? x.x : -x.x, upb ? x.y : -x.y);

@@ -262,7 +262,8 @@ static std::mutex g_jit_mu;
 static std::unordered_map<std::string, std::shared_ptr<Cubin>> g_cubins;
 
 static std::shared_ptr<Cubin> compile_cubin(const std::string& gen_src, bool fp32) {
-    std::string src = std::string(kEmbArgs) + "\n" + kEmbLog + "\n" + kEmbChacha + "\n" + kEmbRt + "\n" + gen_src;
+    std::string src = std::string(kEmbArgs) + "\n" + kEmbLog + "\n" + kEmbChacha + "\n" + kEmbShift + "\n" + kEmbRt +
+                      "\n" + gen_src;
     const std::string key = std::string(fp32 ? "f32|" : "f64|") + src;
     {
         std::lock_guard<std::mutex> g(g_jit_mu);
