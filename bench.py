@@ -361,6 +361,10 @@ def run_engine(args):
     # 2^20 paths x 365 steps, FP32 forward + reverse sweep, against the plain
     # FP64 GPU forward at the same size
     adjoint = adjoint_legs(args, stream, flush, min(npaths, 1 << 20)) if args.adjoint else None
+    # and the target's own configuration: the 4096 uneven instances, forward
+    # and forward+adjoint in one graph-captured launch each, against 4096
+    # per-instance FP64 forward launches
+    batched = batched_legs(args, stream, flush) if args.batched else None
 
     # roofline: SFU bound; peak measured by a MUFU throughput probe
     peak = C.c_double()
@@ -388,6 +392,7 @@ def run_engine(args):
             "fp64_gpu": fp64,
             "sobol_shift_fp32": shift_leg,
             "fwd_adjoint": adjoint,
+            "batched": batched,
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
@@ -682,14 +687,14 @@ def batched_legs(args, stream, flush):
     po = sde_sim_rs.Plan(OU_P, params=["theta", "m", "s"], payoffs=["X"], precision="fp64", output="none")
     ps = int(np.sum(steps.astype(np.uint64) * paths))
 
-    def fp64_launches():
+    def fp64_launches(count=len(tid)):
         res = []
-        for i in range(len(tid)):
+        for i in range(count):
             plan = pg if tid[i] == 0 else po
             res.append(plan.run(np.arange(steps[i] + 1) / steps[i], {"X": x0[i, 0]}, int(paths[i]),
                                 seed=int(seeds[i]), params=params[i, :len(plan.params)], stream=stream))
         return res
-    fp64_launches()[-1].wait()   # warm: both plans loaded
+    fp64_launches(64)[-1].wait()   # warm: both plans loaded (the first 64 instances)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     res = fp64_launches()
@@ -887,6 +892,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="heston_rqmc: leave out the fwd+adjoint legs")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="heston_rqmc: leave out the batched-instance legs")
     ap.add_argument("--scheme", default="euler", choices=["euler", "runge-kutta"],
                     help="adjoint: the scheme whose recursion the reverse sweep runs")
     ap.add_argument("--cuda-cores-only", action="store_true",
