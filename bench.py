@@ -396,10 +396,10 @@ def run_engine(args):
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
-                         # ncu (1 pass, full size): 490.5 KB DRAM read (the Sobol
-                         # tables and masks), 0 B written
-                         "traffic": 490.5e3,
-                         "traffic_source": "profiles/sde_step_euler_fp32_sobolxor_heston_rqmc.md (full-size capture)",
+                         # ncu (1 pass, full size, 8 launches): 0.48 MB DRAM read
+                         # per launch (the Sobol tables and masks), 0 B written
+                         "traffic": 481.5e3,
+                         "traffic_source": "profiles/bench_default_heston_rqmc_launch_list.md (full-size capture)",
                          "peak_source": "measured by sde_probe_sfu_peak (MUFU throughput probe)",
                          "algorithmic_ops_per_launch": sfu_ops},
             "cpu_baseline": {"value": cpu_v, "unit": "path-steps/s", "cores": threads,
@@ -471,7 +471,8 @@ def _timed_runs(fn, steps, stream, flush):
     return [a.elapsed_time(b) for a, b in ev], out
 
 
-def _chacha_roofline(path_steps_per_s, blocks_per_path_step, note, traffic):
+def _chacha_roofline(path_steps_per_s, blocks_per_path_step, note, traffic,
+                     source="profiles/sde_batch_and_adjoint_pseudo.md (full-size one-pass capture)"):
     """Roofline of a pseudo-random kernel: the ChaCha8 blocks it consumes per
     second against the GPU's block rate measured by sde_probe_chacha8_rate
     (the reference's generator is the bound: ALU / issue)."""
@@ -482,7 +483,7 @@ def _chacha_roofline(path_steps_per_s, blocks_per_path_step, note, traffic):
     achieved = path_steps_per_s * blocks_per_path_step
     return {"bound": "alu (ChaCha8)", "achieved": achieved / 1e9, "peak": peak.value / 1e9, "unit": "Gblock/s",
             "frac": achieved / peak.value, "traffic": traffic,
-            "traffic_source": "profiles/sde_batch_and_adjoint_pseudo.md (full-size one-pass capture)",
+            "traffic_source": source,
             "peak_source": "measured by sde_probe_chacha8_rate (every thread generates its own blocks)",
             "algorithmic_blocks_per_path_step": blocks_per_path_step, "note": note}
 
@@ -842,7 +843,14 @@ def adjoint_legs(args, stream, flush, n, scheme="euler"):
                      "gradient_fp32_minus_fp64": dict(zip(names, [float(x) for x in (m[1:] - g64[1:])])),
                      "ms": ta, "fp64_fwd_ms": tf,
                      "e2e_path_steps_per_s": n * ADJ_STEPS / statistics.median(e2e_t),
-                     "clocks": clk.summary(), "n_estimates": 1 + len(names)}
+                     "clocks": clk.summary(), "n_estimates": 1 + len(names),
+                     # the generator's roofline: one u64 per Wiener index and
+                     # path-step; DRAM bytes per launch from the ncu launch
+                     # list at 2^20 paths (Euler)
+                     "roofline": _chacha_roofline(
+                         thr_a, len(eqs) / 8.0, "forward draws plus the reverse sweep over stored increments",
+                         {"gbm": 2.067e9 + 1.343e9, "heston": 4.671e9 + 2.922e9}[name] if scheme == "euler" else None,
+                         "profiles/bench_default_heston_rqmc_launch_list.md (full-size one-pass capture)")}
     out["config"] = {"paths": n, "steps": ADJ_STEPS, "ckpt_every": 19, "rng": "pseudo (ChaCha8)",
                      "scheme": scheme, "l2": "flushed (256 MiB write) between timed launches",
                      "model": "equal_rmse_speedup: RMSE^2 = se^2 N/N' + bias^2 with the FP64 forward's se "
@@ -871,9 +879,9 @@ def run_adjoint(args):
             _chacha_roofline(g["fwd_adjoint_path_steps_per_s"], 1.0 / 8.0,
                              "the forward pass draws one u64 per path-step; the reverse sweep reads the stored "
                              "increments back and adds the recompute and adjoint arithmetic",
-                             # ncu (1 pass, GBM at 2^20 paths): 2.07 GB written (increments and
-                             # checkpoints) + 1.35 GB read (the rest of the increments hit L2)
-                             2.07e9 + 1.35e9),
+                             # ncu (1 pass, GBM at 2^20 paths): 2.067 GB written (increments,
+                             # checkpoints, segment spills) + 1.343 GB read
+                             2.067e9 + 1.343e9),
             None, out)
 
 
