@@ -447,12 +447,7 @@ struct Gen {
             if (uses_chacha()) {
                 int pos = g * NI + k, b = pos / 8, w = (pos % 8) * 2;
                 if (!block_done[b]) {
-                    // the shifted-Sobol kernel is bound by the ALU pipe: its
-                    // block's adds go to the FMA pipe
-                    if (grp_shift)
-                        o.l("sde_chacha8_block_m(" + V("key") + ", blk0 + " + S(b) + "ull, " + V("B", b) + ", one);");
-                    else
-                        o.l("sde_chacha8_block(" + V("key") + ", blk0 + " + S(b) + "ull, " + V("B", b) + ");");
+                    o.l("sde_chacha8_block(" + V("key") + ", blk0 + " + S(b) + "ull, " + V("B", b) + ");");
                     block_done[b] = true;
                 }
                 o.l("const sde_u64 " + V("r", k) + " = sde_pair(" + V("B", b) + "[" + S(w) + "], " + V("B", b) + "[" +
@@ -1266,7 +1261,6 @@ struct Gen {
         o.l("extern \"C\" __global__ void __launch_bounds__(" + S(sp.block) + ") " + name + "(const sde_args a) {");
         o.ind++;
         shared_prologue(o);
-        if (grp_shift) o.l("const sde_u32 one = (sde_u32)a.one;");
         for (int j = 0; j < ppt; ++j) {
             lane(j);
             lane_prologue(o);

@@ -44,9 +44,7 @@ typedef struct sde_args {
     int mask_stride;          /* words per replicate row of masks (multiple of 32)  */
     float udt_f, usdt_f;      /* the FP32 step and its square root when every
                                  step of the grid has them (uniform-grid kernels) */
-    int one;                  /* 1: a multiplier the compiler cannot fold, so
-                                 ChaCha8 adds written as multiply-adds issue on
-                                 the FMA pipe (the shifted-Sobol kernel)       */
+    int pad1;
     sde_u64 tc_wait_cycles;   /* tensor-core step, several threads per path: SM
                                  clocks the A-ready wait lasts before it gives up
                                  (0: about 1 s, the other waits' budget)         */

@@ -42,16 +42,6 @@ SDE_CC_FN void sde_seed_from_u64(sde_u64 s, sde_u32 k[8]) {
     a += b; d ^= a; d = sde_rotl(d, 8);             \
     c += d; b ^= c; b = sde_rotl(b, 7);
 
-/* The same quarter round with its adds written as b * one + a, one = 1
- * held in a register the compiler cannot see through (a launch argument):
- * they issue as integer multiply-adds on the FMA pipe instead of the ALU
- * pipe, which the xors and rotates keep busy. */
-#define SDE_QRM(a, b, c, d, one)                    \
-    a = b * one + a; d ^= a; d = sde_rotl(d, 16);   \
-    c = d * one + c; b ^= c; b = sde_rotl(b, 12);   \
-    a = b * one + a; d ^= a; d = sde_rotl(d, 8);    \
-    c = d * one + c; b ^= c; b = sde_rotl(b, 7);
-
 #define SDE_CC0 0x61707865u
 #define SDE_CC1 0x3320646eu
 #define SDE_CC2 0x79622d32u
@@ -72,26 +62,6 @@ SDE_CC_FN void sde_chacha8_block(const sde_u32 k[8], sde_u64 ctr, sde_u32 o[16])
     o[0] = x0 + SDE_CC0; o[1] = x1 + SDE_CC1; o[2] = x2 + SDE_CC2; o[3] = x3 + SDE_CC3;
     o[4] = x4 + k[0]; o[5] = x5 + k[1]; o[6] = x6 + k[2]; o[7] = x7 + k[3];
     o[8] = x8 + k[4]; o[9] = x9 + k[5]; o[10] = x10 + k[6]; o[11] = x11 + k[7];
-    o[12] = x12 + c0; o[13] = x13 + c1; o[14] = x14; o[15] = x15;
-}
-
-/* sde_chacha8_block with its adds on the FMA pipe (SDE_QRM); one must be 1.
- * Same words. */
-SDE_CC_FN void sde_chacha8_block_m(const sde_u32 k[8], sde_u64 ctr, sde_u32 o[16], sde_u32 one) {
-    const sde_u32 c0 = (sde_u32)ctr, c1 = (sde_u32)(ctr >> 32);
-    sde_u32 x0 = SDE_CC0, x1 = SDE_CC1, x2 = SDE_CC2, x3 = SDE_CC3;
-    sde_u32 x4 = k[0], x5 = k[1], x6 = k[2], x7 = k[3];
-    sde_u32 x8 = k[4], x9 = k[5], x10 = k[6], x11 = k[7];
-    sde_u32 x12 = c0, x13 = c1, x14 = 0u, x15 = 0u;
-    SDE_CC_UNROLL for (int r = 0; r < 4; ++r) {
-        SDE_QRM(x0, x4, x8, x12, one) SDE_QRM(x1, x5, x9, x13, one)
-        SDE_QRM(x2, x6, x10, x14, one) SDE_QRM(x3, x7, x11, x15, one)
-        SDE_QRM(x0, x5, x10, x15, one) SDE_QRM(x1, x6, x11, x12, one)
-        SDE_QRM(x2, x7, x8, x13, one) SDE_QRM(x3, x4, x9, x14, one)
-    }
-    o[0] = x0 + SDE_CC0; o[1] = x1 + SDE_CC1; o[2] = x2 + SDE_CC2; o[3] = x3 + SDE_CC3;
-    o[4] = k[0] * one + x4; o[5] = k[1] * one + x5; o[6] = k[2] * one + x6; o[7] = k[3] * one + x7;
-    o[8] = k[4] * one + x8; o[9] = k[5] * one + x9; o[10] = k[6] * one + x10; o[11] = k[7] * one + x11;
     o[12] = x12 + c0; o[13] = x13 + c1; o[14] = x14; o[15] = x15;
 }
 

@@ -625,7 +625,6 @@ static sde_result* run(sde_plan* p, const sde_run_args& a) {
 
     sde_args A;
     std::memset(&A, 0, sizeof A);
-    A.one = 1;
     A.times = (const double*)dptr(h_times);
     A.dts = (const double*)dptr(h_dts);
     A.sqrt_dts = (const double*)dptr(h_sdts);

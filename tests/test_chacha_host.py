@@ -20,7 +20,6 @@ SHIM = r"""
 #include "sde_chacha.h"
 void seed(unsigned long long s, sde_u32* k) { sde_seed_from_u64(s, k); }
 void block(const sde_u32* k, unsigned long long ctr, sde_u32* o) { sde_chacha8_block(k, ctr, o); }
-void block_m(const sde_u32* k, unsigned long long ctr, sde_u32* o, sde_u32 one) { sde_chacha8_block_m(k, ctr, o, one); }
 """
 
 COUNTERS = [0, 1, 2, 7, 1000, 2**31, 2**32 - 1, 2**32, 2**32 + 5, 2**40 + 3, 2**63 + 7, 2**64 - 1]
@@ -39,7 +38,6 @@ def lib(tmp_path_factory):
     L = C.CDLL(str(so))
     L.seed.argtypes = [C.c_uint64, C.c_void_p]
     L.block.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
-    L.block_m.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint32]
     return L
 
 
@@ -80,15 +78,3 @@ def test_stream_u64_order(lib, oracle):
     lib.seed(99, k.ctypes.data)
     words = np.concatenate([_blk(lib, k, b) for b in range(4)]).astype(np.uint64)
     assert np.array_equal(words[0::2] | (words[1::2] << np.uint64(32)), oracle.chacha8_u64(99, 0, 32))
-
-
-def test_multiply_add_block_is_the_same_block(lib, oracle):
-    """The shifted-Sobol kernel's block (adds as multiply-adds by a one the
-    compiler cannot fold) gives the same words."""
-    rng = np.random.default_rng(11)
-    for _ in range(20):
-        key = rng.integers(0, 2**32, 8, dtype=np.uint64).astype(np.uint32)
-        for ctr in COUNTERS:
-            o = np.zeros(16, dtype=np.uint32)
-            lib.block_m(key.ctypes.data, ctr, o.ctypes.data, 1)
-            assert np.array_equal(o, _blk(lib, key, ctr)), (key, ctr)
