@@ -365,6 +365,12 @@ def run_engine(args):
     # and forward+adjoint in one graph-captured launch each, against 4096
     # per-instance FP64 forward launches
     batched = batched_legs(args, stream, flush) if args.batched else None
+    # the reference's own configuration (GBM, 10,000 paths, FP64, full
+    # filtration) and the memory-bound 64-dim basket, each as its own line
+    others = {}
+    if rank == 0 and args.others:
+        others["gbm_full"] = collected(run_gbm_full, args)
+        others["basket"] = collected(run_basket, args)
 
     # roofline: SFU bound; peak measured by a MUFU throughput probe
     peak = C.c_double()
@@ -393,6 +399,7 @@ def run_engine(args):
             "sobol_shift_fp32": shift_leg,
             "fwd_adjoint": adjoint,
             "batched": batched,
+            "other_configs": others or None,
             "gpu_launches": 3 * args.steps,
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": peak.value / 1e9,
                          "unit": "Gop/s", "frac": achieved / peak.value,
@@ -495,7 +502,21 @@ def _common(args, workload, metric, value, ms, dtype, clocks, e2e, launches, roo
             "config": dict(workload=workload, l2="flushed (256 MiB write) between timed steps", **extra),
             "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "cpu_baseline": cpu}
-    print(json.dumps(line), flush=True)
+    if getattr(args, "collect", None) is not None:
+        args.collect.append(line)
+    else:
+        print(json.dumps(line), flush=True)
+
+
+def collected(run, args):
+    """Runs another configuration's bench and returns its line as a dict
+    (nested in the default line) instead of printing it."""
+    args.collect = []
+    try:
+        run(args)
+        return args.collect[-1]
+    finally:
+        args.collect = None
 
 
 def run_gbm_full(args):
@@ -902,6 +923,8 @@ def main():
                     help="heston_rqmc: leave out the fwd+adjoint legs")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="heston_rqmc: leave out the batched-instance legs")
+    ap.add_argument("--no-others", dest="others", action="store_false",
+                    help="heston_rqmc: leave out the GBM full-filtration and 64-dim basket lines")
     ap.add_argument("--scheme", default="euler", choices=["euler", "runge-kutta"],
                     help="adjoint: the scheme whose recursion the reverse sweep runs")
     ap.add_argument("--cuda-cores-only", action="store_true",
