@@ -465,17 +465,24 @@ def _peaks():
 
 
 def _timed_runs(fn, steps, stream, flush):
+    """CUDA-event time of each of `steps` runs, L2 flushed before each
+    (outside the events).  Only the latest run's result is kept alive: the
+    one before it is released once the next is queued (its release waits for
+    its own work only), so device memory holds at most two runs' buffers
+    (a 64-dim basket run holds 17 GB).  Returns (ms list, [last result])."""
     import torch
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    out = []
+    last = None
     torch.cuda.synchronize()
     for k in range(steps):
         flush.fill_(k & 0xFF)
         ev[k][0].record(stream)
-        out.append(fn())
+        r = fn()
         ev[k][1].record(stream)
+        last = r
+        del r
     torch.cuda.synchronize()
-    return [a.elapsed_time(b) for a, b in ev], out
+    return [a.elapsed_time(b) for a, b in ev], [last]
 
 
 def _chacha_roofline(path_steps_per_s, blocks_per_path_step, note, traffic,
