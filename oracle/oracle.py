@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/sde_oracle.c).
 
-TEST INFRASTRUCTURE ONLY.  This is the checker of the GPU engine and the
-timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's
+TEST INFRASTRUCTURE ONLY.  The oracle: what the GPU engine's parity tests
+compare with, and the timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's
 cpu_baseline / reference arm import it; the product package never does.
 
 The oracle restates the sde-sim-rs hot path (src/sim, src/proc, src/rng,

@@ -1,7 +1,7 @@
 /*
  * sde_oracle.c -- CPU restatement of the sde-sim-rs path-simulation
- * algorithm.  TEST INFRASTRUCTURE ONLY: the checker for the GPU engine and
- * the timed CPU baseline; never part of the product path.
+ * algorithm.  TEST INFRASTRUCTURE ONLY: what the GPU engine's parity tests
+ * compare with, and the timed CPU baseline; never part of the product path.
  *
  * Compile with -ffp-contract=off: the reference (Rust) never contracts
  * a*b+c into a fused multiply-add, and aarch64 gcc would otherwise do so.

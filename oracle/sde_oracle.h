@@ -1,8 +1,8 @@
 /*
  * sde_oracle.h -- CPU restatement of the sde-sim-rs path-simulation algorithm.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU engine:
- * only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+ * TEST INFRASTRUCTURE ONLY.  The GPU engine's parity tests compare with this
+ * library; only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
  * arm may load it.  The product (libsdegpu.so) never links or calls it.
  *
  * It restates, in plain C, the reference crate's hot path:
