@@ -56,3 +56,15 @@ def test_profile_summaries_cite_committed_commands():
         assert all("--clock-control none" in ln for ln in ncu), n
         for script in set(re.findall(r"python ([\w/.-]+\.py)", text)):
             assert os.path.isfile(os.path.join(ROOT, script)) and not script.startswith("_work"), (n, script)
+
+
+def test_equal_rmse_speedup_model():
+    """RMSE^2 = se^2 N/N' + bias^2: FP32 matches the FP64 RMSE at N with
+    N' = N se^2 / (se^2 - bias^2) paths, so the time ratio is
+    (thr32 / thr64)(1 - bias^2 / se^2); 0 once the bias alone reaches se."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.equal_rmse_speedup(100.0, 1.0, 0.0, 0.5) == 100.0
+    assert abs(bench.equal_rmse_speedup(100.0, 1.0, 0.25, 0.5) - 75.0) < 1e-12
+    assert bench.equal_rmse_speedup(100.0, 1.0, 0.5, 0.5) == 0.0
+    assert bench.equal_rmse_speedup(100.0, 1.0, 0.1, 0.0) is None
