@@ -166,9 +166,12 @@ int sde_plan_create(const char* const* equations, int32_t n_equations,
 /* Pathwise adjoint (no counterpart in the reference, which has no
  * derivatives): a plan whose runs also return d E[payoffs[0]] / d params
  * (grad_params, names of declared parameters) and / d X0 (grad_x0, process
- * names), by a reverse sweep of Euler-Maruyama recomputed from checkpoints
- * every opts->ckpt_every steps.  Euler only, no algebraic processes.  The
- * run's estimates are [payoffs..., grad_params..., grad_x0...] per
+ * names), by a reverse sweep of the step recursion -- Euler-Maruyama
+ * (src/sim/euler.rs:5-37) or Runge-Kutta (src/sim/runge_kutta.rs:17-97,
+ * its sign held fixed; in the reference's semantics the name->value cache
+ * that the next stage 1 reads is differentiated as state) -- recomputed
+ * from checkpoints every opts->ckpt_every steps.  No algebraic processes.
+ * The run's estimates are [payoffs..., grad_params..., grad_x0...] per
  * replicate (per-path sums and sums of squares).                          */
 int sde_plan_create_adjoint(const char* const* equations, int32_t n_equations,
                             const char* const* param_names, int32_t n_params,
@@ -275,11 +278,15 @@ int sde_run_estimates_static(sde_plan* plan, const double* times, int32_t n_time
 
 /* ---- batched instances ---------------------------------------------------
  * No counterpart in the reference (one universe per simulate call): many
- * independent instances of a few templates (plans from sde_plan_create,
- * pseudo-random, same precision), each with its own uniform step count,
- * horizon, path count, seed, initial values and parameters, run by one
- * persistent work-queue kernel captured in a CUDA graph.  Paths per thread
- * and block shape come from a timing autotuner at prepare time.           */
+ * independent instances of a few templates (plans from sde_plan_create or
+ * sde_plan_create_adjoint, pseudo-random, same precision), each with its
+ * own uniform step count, horizon, path count, seed, initial values and
+ * parameters, run by one persistent work-queue kernel captured in a CUDA
+ * graph.  Paths per thread and block shape come from a timing autotuner at
+ * prepare time.  An adjoint template's instances also return the gradients
+ * of its payoff 0, as its plan's runs do; they take at most 4096 steps
+ * (checkpoints every ceil(sqrt(steps)) steps in per-thread arrays; more is
+ * SDE_ERR_UNSUPPORTED).                                                   */
 typedef struct sde_batch sde_batch;
 typedef struct sde_batch_job sde_batch_job;
 
@@ -307,7 +314,8 @@ int sde_batch_prepare(sde_batch* batch, const sde_batch_instances* inst, int32_t
 /* Replays the graph: one persistent launch over every instance. */
 int sde_batch_job_run(sde_batch_job* job, void* stream);
 /* Waits; per instance and payoff: sum and sum of squares over its paths,
- * arrays [n_instances][n_payoffs] (n_payoffs = the largest template's).  */
+ * arrays [n_instances][n_payoffs] (n_payoffs = the largest template's
+ * estimate count: payoffs, plus gradients for an adjoint template).      */
 int sde_batch_job_results(sde_batch_job* job, double* host_sum, double* host_sumsq);
 int sde_batch_job_info(const sde_batch_job* job, int32_t* block, int32_t* paths_per_thread,
                        int32_t* n_items, uint64_t* path_steps, int32_t* n_payoffs);
