@@ -189,10 +189,11 @@ class Plan:
                  chunked: str = "auto"):
         """grad_params / grad_x0 make an adjoint plan: each run also returns
         the pathwise derivatives of E[payoffs[0]] with respect to those
-        parameters and initial values (Euler-Maruyama, checkpoints every
-        ckpt_every steps, default 19); the forward pass's increments are kept
-        in device memory for the reverse sweep when they fit in a quarter of
-        the free memory (adjoint_recompute=True draws them again instead).
+        parameters and initial values (Euler-Maruyama or Runge-Kutta in
+        either semantics, checkpoints every ckpt_every steps, default 19);
+        the forward pass's increments are kept in device memory for the
+        reverse sweep when they fit in a quarter of the free memory
+        (adjoint_recompute=True draws them again instead).
         tensor_cores=True lowers the dW
         terms of an FP32 Euler universe whose diffusions are constant * own
         process (correlated GBM) to one tcgen05 product per 128 paths, with

@@ -1,13 +1,16 @@
 """Many independent SDE instances in one persistent, graph-captured launch.
 
 The reference simulates one process universe per call
-(src/sim/mod.rs:20-92).  ``Batch`` takes a few forward plans as templates
+(src/sim/mod.rs:20-92).  ``Batch`` takes a few plans as templates
 (e.g. one GBM and one Ornstein-Uhlenbeck universe written with named
 parameters) and runs thousands of instances of them -- each with its own
 uniform step count, horizon, path count, seed, initial values and parameter
 values -- as one work-queue kernel.  ``prepare`` picks the block shape and
 paths per thread by timing the candidates on the actual instances, then
 captures the launch in a CUDA graph; ``BatchJob.run`` replays it.
+Adjoint plans (``Plan(..., grad_params=..., grad_x0=...)``) are templates
+too: their instances also return the gradients of payoff 0 (at most 4096
+steps each).
 """
 from __future__ import annotations
 
