@@ -531,3 +531,25 @@ def test_roofline_probes(engine):
     clock = 2.2e9  # above the part's top SM clock
     assert 0 < ops.value <= 16 * sms * clock
     assert 0 < blocks.value <= sms * clock
+
+
+@pytest.mark.parametrize("dim", [4, 8, 16, 32])
+@pytest.mark.parametrize("ppt", [1, 2])
+def test_shifted_sobol_chunk_loop_widths(engine, oracle, dim, ppt):
+    """The FP32 kernel on the reference's shifted Sobol points walks
+    32-dimension chunks with rolled inner step groups for 1, 2, 4, ..., 32
+    stochastic indices: correlated baskets of 4 to 32 indices (8 to 1 steps
+    per chunk), one and two paths per thread, a path offset inside a warp,
+    against the FP64 oracle on the same points and shifts."""
+    from bench import basket_equations
+    eqs, _, _, _ = basket_equations(dim)
+    init = {f"S{i + 1}": 100.0 for i in range(dim)}
+    times = np.linspace(0.0, 1.0, 21)
+    n, offset, seed = 300, 37, 9
+    plan = engine.Plan(eqs, rng="sobol", scramble="shift", precision="fp32", paths_per_thread=ppt)
+    gpu = plan.run(times, init, n, seed=seed, path_offset=offset).values()[0]
+    ref = oracle.Universe(eqs).simulate(times, init, offset, offset + n, rng=oracle.SOBOL, seed=seed,
+                                        threads=THREADS)
+    rel = np.abs(gpu - ref) / np.abs(ref)
+    assert np.mean(rel < 1e-3) > 0.99, np.percentile(rel, [50, 99, 100])
+    assert rel.max() < 1e-2
