@@ -860,6 +860,16 @@ def adjoint_legs(args, stream, flush, n, scheme="euler"):
         g64 = a64.run(T, init, n, seed=42, params=params, stream=stream).estimates()[0][0] / n
         ta, tf = statistics.median(ms_a), statistics.median(ms_f)
         thr_a, thr_f = n * ADJ_STEPS / (ta * 1e-3), n * ADJ_STEPS / (tf * 1e-3)
+        # the same adjoint with its memory bounded by the checkpoints alone:
+        # the reverse sweep draws the increments again instead of keeping
+        # the forward pass's (N x steps x indices x 4 B) in device memory;
+        # the same increments, so the same estimates bit for bit
+        rec = sde_sim_rs.Plan(eqs, grad_params=gp, grad_x0=gx, precision="fp32", adjoint_recompute=True, **kw)
+        one_r = lambda: rec.run(T, init, n, seed=42, params=params, stream=stream)
+        one_r().wait()
+        ms_r, rr = _timed_runs(one_r, max(3, args.steps // 2), stream, flush)
+        same = bool(np.array_equal(rr[-1].estimates()[0], ra[-1].estimates()[0]))
+        thr_r = n * ADJ_STEPS / (statistics.median(ms_r) * 1e-3)
         names = gp + gx
         out[name] = {"fwd_adjoint_path_steps_per_s": thr_a, "fp64_fwd_path_steps_per_s": thr_f,
                      "throughput_ratio_fp32_fwd_adj_vs_fp64_fwd": thr_a / thr_f,
@@ -870,6 +880,15 @@ def adjoint_legs(args, stream, flush, n, scheme="euler"):
                      "gradient_se": dict(zip(names, [float(x) for x in se[1:]])),
                      "gradient_fp32_minus_fp64": dict(zip(names, [float(x) for x in (m[1:] - g64[1:])])),
                      "ms": ta, "fp64_fwd_ms": tf,
+                     "increments_kept_bytes": n * ADJ_STEPS * (len(eqs) + (scheme != "euler")) * 4,
+                     "checkpoints_only": {"fwd_adjoint_path_steps_per_s": thr_r,
+                                          "ms": statistics.median(ms_r),
+                                          "throughput_ratio_vs_fp64_fwd": thr_r / thr_f,
+                                          "equal_rmse_speedup": equal_rmse_speedup(thr_r, thr_f, float(m[0]) - p64,
+                                                                                   se64),
+                                          "checkpoint_bytes": n * ((ADJ_STEPS + 18) // 19) * len(eqs) *
+                                          (1 if scheme == "euler" else 2) * 4,
+                                          "estimates_equal_to_kept_increments": same},
                      "e2e_path_steps_per_s": n * ADJ_STEPS / statistics.median(e2e_t),
                      "clocks": clk.summary(), "n_estimates": 1 + len(names),
                      # the generator's roofline: one u64 per Wiener index and
