@@ -175,6 +175,12 @@ def test_batch_lowering_compiles(engine):
     to = engine.Plan(["dX = (theta * (m - X)) * dt + (s) * dW1"], params=["theta", "m", "s"],
                      payoffs=["X", "X^2"], precision="fp32", output="none", scheme="runge-kutta")
     Batch([tg, to])
+    # adjoint plans are templates too (Euler and Runge-Kutta), beside forward ones
+    ag = engine.Plan(["dX = (mu * X) * dt + (sigma * X) * dW1"], params=["mu", "sigma"], payoffs=["X"],
+                     grad_params=["mu", "sigma"], grad_x0=["X"], precision="fp32", output="none")
+    ar = engine.Plan(["dX = (theta * (m - X)) * dt + (s) * dW1"], params=["theta", "m", "s"], payoffs=["X"],
+                     grad_params=["theta"], precision="fp32", output="none", scheme="runge-kutta")
+    Batch([tg, ag, ar])
     with pytest.raises(Exception, match="pseudo-random"):
         Batch([engine.Plan(["dX = (0.1) * dW1"], payoffs=["X"], rng="sobol")])
     with pytest.raises(ValueError, match="share one precision"):
