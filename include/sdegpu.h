@@ -308,7 +308,9 @@ int sde_batch_create(const sde_plan* const* templates, int32_t n_templates, sde_
 int sde_batch_destroy(sde_batch* batch);
 /* Uploads the instances, builds the work queue (longest instances first),
  * picks (block, paths per thread) by timing each candidate when autotune is
- * nonzero, and captures the launch in a CUDA graph.                      */
+ * positive (0: the first candidate; -1 - v: candidate v, of the shapes
+ * (128, 1), (256, 1), (128, 2), (256, 2), (128, 4)), and captures the
+ * launch in a CUDA graph.                                                 */
 int sde_batch_prepare(sde_batch* batch, const sde_batch_instances* inst, int32_t autotune,
                       void* stream, sde_batch_job** out_job);
 /* Replays the graph: one persistent launch over every instance. */

@@ -1522,7 +1522,11 @@ int sde_batch_prepare(sde_batch* b, const sde_batch_instances* in, int32_t autot
         j->args.counter = j->counter.as<unsigned>();
         batch_loaded(b);
         int best = 0;
-        if (autotune) {
+        if (autotune < 0) {
+            // a fixed candidate, -1 - autotune (tests of each shape)
+            best = -1 - autotune;
+            if (best >= (int)kBatchVariants.size()) fail(SDE_ERR_INVALID, "no such candidate shape");
+        } else if (autotune) {
             float best_ms = 1e30f;
             for (int v = 0; v < (int)kBatchVariants.size(); ++v) {
                 build_items(j.get(), *in, v, s);

@@ -77,10 +77,15 @@ class Batch:
             N._lib.sde_batch_destroy(h)
             self._h = C.c_void_p()
 
+    # the candidate (block, paths per thread) shapes, in the engine's order
+    SHAPES = ((128, 1), (256, 1), (128, 2), (256, 2), (128, 4))
+
     def prepare(self, template_id, n_steps, t_end, n_paths, seed, x0, params, *, autotune: bool = True,
-                stream=None) -> BatchJob:
+                shape: int | None = None, stream=None) -> BatchJob:
         """x0: [n, x0_stride] initial values by process index of the
-        instance's template; params: [n, param_stride] by parameter index."""
+        instance's template; params: [n, param_stride] by parameter index.
+        shape (an index into SHAPES) fixes the launch shape instead of
+        timing the candidates."""
         tid = np.ascontiguousarray(template_id, dtype=np.int32)
         n = len(tid)
         steps = np.ascontiguousarray(np.broadcast_to(n_steps, (n,)), dtype=np.int32)
@@ -97,6 +102,6 @@ class Batch:
         ins.x0, ins.x0_stride = x0a.ctypes.data, x0a.shape[1]
         ins.params, ins.param_stride = pa.ctypes.data, pa.shape[1]
         h = C.c_void_p()
-        N.check(_lib().sde_batch_prepare(self._h, C.byref(ins), 1 if autotune else 0, _stream(stream),
-                                         C.byref(h)))
+        mode = -1 - int(shape) if shape is not None else (1 if autotune else 0)
+        N.check(_lib().sde_batch_prepare(self._h, C.byref(ins), mode, _stream(stream), C.byref(h)))
         return BatchJob(h, self, n)

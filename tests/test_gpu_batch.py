@@ -175,3 +175,34 @@ def test_batched_adjoint_greeks_and_limits(engine):
     with pytest.raises(Exception, match="at most 4096 steps"):
         b.prepare(np.zeros(1, np.int32), 4097, 1.0, 256, np.zeros(1, np.uint64), np.full((1, 1), 100.0),
                   np.array([[0.05, 0.2]]))
+
+
+@pytest.mark.parametrize("adjoint", [False, True], ids=["forward", "fwd_adjoint"])
+def test_every_launch_shape_gives_the_same_instances(engine, adjoint):
+    """Each candidate (block, paths per thread) shape the autotuner may pick
+    only regroups paths: per-instance estimates agree with the first shape's
+    to rounding of the compensated sums, forward and forward+adjoint (whose
+    template steps a thread's paths one after another)."""
+    from sde_sim_rs.batch import Batch
+    n = 40
+    tid, steps, paths, seeds, x0, params = make_instances(n, 31, max_steps=150, max_log2_paths=11)
+    kw = dict(precision="fp32", output="none")
+    if adjoint:
+        tg = engine.Plan(GBM_T, params=["mu", "sigma"], payoffs=["max(X - 100, 0)"], grad_params=["mu", "sigma"],
+                         grad_x0=["X"], **kw)
+        to = engine.Plan(OU_T, params=["theta", "m", "s"], payoffs=["X"], grad_params=["theta", "m", "s"],
+                         grad_x0=["X"], scheme="runge-kutta", **kw)
+    else:
+        tg = engine.Plan(GBM_T, params=["mu", "sigma"], payoffs=["max(X - 100, 0)"], **kw)
+        to = engine.Plan(OU_T, params=["theta", "m", "s"], payoffs=["X"], **kw)
+    b = Batch([tg, to])
+    out = []
+    for shape in range(len(Batch.SHAPES)):
+        job = b.prepare(tid, steps, 1.0, paths, seeds, x0, params, shape=shape)
+        assert (job.block, job.paths_per_thread) == Batch.SHAPES[shape]
+        out.append(job.run().results())
+    for s, q in out[1:]:
+        np.testing.assert_allclose(s, out[0][0], rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(q, out[0][1], rtol=1e-9, atol=1e-9)
+    with pytest.raises(Exception, match="no such candidate"):
+        b.prepare(tid, steps, 1.0, paths, seeds, x0, params, shape=len(Batch.SHAPES))
