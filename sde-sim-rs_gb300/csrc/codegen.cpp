@@ -1106,16 +1106,19 @@ struct Gen {
     // Sobol high parts of the 32-dimension chunks of the group starting at
     // chunk `first` (an expression), fetched a group ahead; chunks past the
     // last step's dimensions are not read (the scramble-mask rows end
-    // there).  The tensor-core step issues the loads eight bits of H at a
-    // time (sde_sobol_hi_unrolled); the CUDA-core kernels loop over H's set
-    // bits, fewer instructions now that the fetch runs a group ahead
-    // (Heston 7.95 -> 7.81 ms, FP32 GBM 1.08 -> 1.01 ms)
+    // there).  The tensor-core step with one thread per path issues the
+    // loads eight bits of H at a time (sde_sobol_hi_unrolled); the others
+    // loop over H's set bits, fewer instructions now that the fetch runs a
+    // group ahead (Heston 7.95 -> 7.81 ms, FP32 GBM 1.08 -> 1.01 ms; the
+    // 64-dim basket with two threads per path 22.14 -> 21.26 ms, while one
+    // thread per path slowed from 25.45 to 28.86 ms with the loop)
     void hv_prefetch(Out& o, const std::string& first) const {
         const std::vector<bool> need = own_chunks();
         for (int c = 0; c < (int)need.size(); ++c)
             if (need[c])
                 o.l("if (32 * (" + first + " + " + S(c) + ") < n_steps * " + S(NI) + ") " + V("hvn", c) +
-                " = " + (mma ? "sde_sobol_hi_unrolled" : "sde_sobol_hi") + "(a.sobol_vt, mask_rep, a.sobol_dims, " + first + " + " + S(c) + ", " +
+                " = " + (mma && mma->split == 1 ? "sde_sobol_hi_unrolled" : "sde_sobol_hi") +
+                "(a.sobol_vt, mask_rep, a.sobol_dims, " + first + " + " + S(c) + ", " +
                 V("H") + ", lane);");
     }
 
