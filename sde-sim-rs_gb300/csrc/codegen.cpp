@@ -1579,27 +1579,54 @@ struct Gen {
         auto inc_at = [&](int k) {
             return "INC[(((sde_u64)rep * n_steps + t) * " + S(NS) + "ull + " + S(k) + "ull) * a.n_paths + i]";
         };
-        // forward pass with checkpoints
-        o.l("for (int t = 0; t < n_steps; ++t) {");
-        o.ind++;
-        o.l("if (t % " + E + " == 0 && active) {");
-        for (int p = 0; p < P; ++p) o.l("  " + ck_at("t / " + E, p) + " = X" + S(p) + ";");
-        if (refc)
-            for (int p = 0; p < P; ++p) o.l("  " + ck_at("t / " + E, P + p) + " = C" + S(p) + ";");
-        o.l("}");
-        step_header(o);
-        uniforms_ra(o);
-        wiener(o);
-        if (rk) step(o);
-        else step_reference(o);
-        if (NS > 0 && !batch) {
-            o.l("if (INC && active) {");
-            for (int k = 0; k < NI; ++k) o.l("  " + inc_at(k) + " = " + inc_store_name(k) + ";");
-            if (rk) o.l("  " + inc_at(NI) + " = sk;");
+        // forward pass with checkpoints.  On the ChaCha8 streams it runs in
+        // groups of whole blocks (8 u64) with every block word a
+        // compile-time index, as the forward kernels do; the segment
+        // recompute below reads the blocks by step (uniforms_ra)
+        const bool grouped = sp.rng == RNG_PSEUDO && NI > 0;
+        const int U = grouped ? group() : 1;
+        std::vector<bool> done(std::max(1, (U * NI) / 8), false);
+        auto fwd_step = [&](int g) {
+            o.l("if (t % " + E + " == 0 && active) {");
+            for (int p = 0; p < P; ++p) o.l("  " + ck_at("t / " + E, p) + " = X" + S(p) + ";");
+            if (refc)
+                for (int p = 0; p < P; ++p) o.l("  " + ck_at("t / " + E, P + p) + " = C" + S(p) + ";");
+            o.l("}");
+            step_header(o);
+            if (grouped) uniforms(o, g, done);
+            else uniforms_ra(o);
+            wiener(o);
+            if (rk) step(o);
+            else step_reference(o);
+            if (NS > 0 && !batch) {
+                o.l("if (INC && active) {");
+                for (int k = 0; k < NI; ++k) o.l("  " + inc_at(k) + " = " + inc_store_name(k) + ";");
+                if (rk) o.l("  " + inc_at(NI) + " = sk;");
+                o.l("}");
+            }
+        };
+        if (grouped) {
+            o.l("for (int t0 = 0; t0 < n_steps; t0 += " + S(U) + ") {");
+            o.ind++;
+            o.l("const sde_u64 blk0 = ((sde_u64)t0 * " + S(NI) + "ull) / 8ull;");
+            for (int b = 0; b < (U * NI) / 8; ++b) o.l("sde_u32 " + V("B", b) + "[16];");
+            for (int g = 0; g < U; ++g) {
+                o.l("{ const int t = t0 + " + S(g) + ";");
+                o.l("if (t < n_steps) {");
+                o.ind++;
+                fwd_step(g);
+                o.ind--;
+                o.l("} }");
+            }
+            o.ind--;
+            o.l("}");
+        } else {
+            o.l("for (int t = 0; t < n_steps; ++t) {");
+            o.ind++;
+            fwd_step(0);
+            o.ind--;
             o.l("}");
         }
-        o.ind--;
-        o.l("}");
         // payoffs and the terminal adjoint of payoff 0
         o.l("const " + R + " tT = " + (batch ? "(" + R + ")n_steps * bdt" : "(" + R + ")__ldg(&a.times[a.T - 1])") + ";");
         for (int k = 0; k < K; ++k)
