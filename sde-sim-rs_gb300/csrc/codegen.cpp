@@ -1579,11 +1579,14 @@ struct Gen {
         auto inc_at = [&](int k) {
             return "INC[(((sde_u64)rep * n_steps + t) * " + S(NS) + "ull + " + S(k) + "ull) * a.n_paths + i]";
         };
-        // forward pass with checkpoints.  On the ChaCha8 streams it runs in
-        // groups of whole blocks (8 u64) with every block word a
-        // compile-time index, as the forward kernels do; the segment
-        // recompute below reads the blocks by step (uniforms_ra)
-        const bool grouped = sp.rng == RNG_PSEUDO && NI > 0;
+        // forward pass with checkpoints.  The plan kernel on the ChaCha8
+        // streams runs it in groups of whole blocks (8 u64) with every block
+        // word a compile-time index, as the forward kernels do (GBM adjoint
+        // 2.055 -> 1.949 ms, Heston 4.171 -> 4.006 ms); the segment
+        // recompute below reads the blocks by step (uniforms_ra).  The
+        // batched template keeps the per-step form: the larger code slowed
+        // the batch, which carries every template (157.9 -> 164.9 ms)
+        const bool grouped = sp.rng == RNG_PSEUDO && NI > 0 && !batch;
         const int U = grouped ? group() : 1;
         std::vector<bool> done(std::max(1, (U * NI) / 8), false);
         auto fwd_step = [&](int g) {
