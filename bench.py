@@ -361,6 +361,9 @@ def run_engine(args):
     # 2^20 paths x 365 steps, FP32 forward + reverse sweep, against the plain
     # FP64 GPU forward at the same size
     adjoint = adjoint_legs(args, stream, flush, min(npaths, 1 << 20)) if args.adjoint else None
+    # the same Greeks through the reference's Runge-Kutta scheme (its cache
+    # semantics), against the plain FP64 Runge-Kutta forward
+    adjoint_rk = adjoint_legs(args, stream, flush, min(npaths, 1 << 20), scheme="runge-kutta") if args.adjoint else None
     # and the target's own configuration: the 4096 uneven instances, forward
     # and forward+adjoint in one graph-captured launch each, against 4096
     # per-instance FP64 forward launches
@@ -398,6 +401,7 @@ def run_engine(args):
             "fp64_gpu": fp64,
             "sobol_shift_fp32": shift_leg,
             "fwd_adjoint": adjoint,
+            "fwd_adjoint_runge_kutta": adjoint_rk,
             "batched": batched,
             "other_configs": others or None,
             "gpu_launches": 3 * args.steps,
